@@ -1,0 +1,300 @@
+"""Benchmark: Taylor-Green vortex 512^3 incompressible step on GB300.
+
+Metric: grid-points x time-steps per second (Mpts*steps/s) of the full time
+step (momentum RHS with 27 compact line solves, AB3 update, divergence,
+FFT Poisson solve, gradient, correction), fields resident in HBM.
+value = the mixed-precision solver (FP32 operators, FP64 state, time
+integration and Poisson FFT); the FP64 solver is reported beside it, together
+with the kinetic-energy difference between the two after the same steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--n 512] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference's path (the
+parity oracle, C++/OpenMP on all host cores) on a bounded sample grid of the
+same workload, and reports the same metric.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "TGV 512^3 Mpts*steps/s (mixed FP32/FP64 step; FP64 step reported beside it)"
+UNIT = "Mpts*steps/s"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """Samples nvidia-smi during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 7:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_oracle_rate(n=96, steps=3):
+    """Oracle TGV AB3 steps on an n^3 sample (all host threads): Mpts*steps/s."""
+    import numpy as np
+    import oracle
+    oracle.build()
+    threads = oracle.Oracle.set_threads(os.cpu_count() or 1)
+    L = 2 * np.pi
+    o = oracle.Oracle(n, n, n, L, L, L)
+    x = np.arange(n) * (L / n)
+    X, Y, Z = x[None, None, :], x[None, :, None], x[:, None, None]
+    ux = np.sin(X) * np.cos(Y) * np.cos(Z)
+    uy = -np.cos(X) * np.sin(Y) * np.cos(Z)
+    uz = np.zeros_like(ux)
+    o.run(ux, uy, uz, 1, 0.002, 1 / 1600.0, 3, 0)  # warm-up
+    t0 = time.perf_counter()
+    o.run(ux, uy, uz, steps, 0.002, 1 / 1600.0, 3, 0)
+    dt = time.perf_counter() - t0
+    return n ** 3 * steps / dt / 1e6, threads, dt
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    n = args.ref_n
+    rate, threads, dt = cpu_oracle_rate(n, max(1, args.steps // 4))
+    sample = "TGV %d^3 AB3 steps (sample of the 512^3 workload; rate per grid point)" % n
+    line = {"impl": "reference", "metric": METRIC, "value": round(rate, 4), "unit": UNIT, "n_gpus": args.gpus,
+            "steps": max(1, args.steps // 4), "warmup": 1, "ms_per_step": round(1e3 * dt / max(1, args.steps // 4), 2),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "tgv_%d^3_ab3_cpu_oracle" % n, "grid": [n, n, n], "re": 1600, "dt": 0.002},
+            "cpu_baseline": {"value": round(rate, 4), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(rate, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def time_steps(torch, solver, steps, stream):
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    solver.step(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def time_kernel(torch, fn, reps, stream):
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    fn()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3 / reps
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import incompact3d_gb300 as x3d
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    x3d.build()
+    n = args.n
+    L = 2 * np.pi
+    N = n ** 3
+    dt = 0.002
+    stream = torch.cuda.current_stream()
+    ctx = x3d.Context(n, n, n, L, L, L)
+    res = {}
+    ke = {}
+    solvers = {}
+    for prec in (["mixed", "fp64"] if args.precision == "both" else [args.precision]):
+        p = x3d.PREC_MIXED if prec == "mixed" else x3d.PREC_FP64
+        s = x3d.Solver(ctx, dt, 1 / 1600.0, itimescheme=3, precision=p)
+        s.init_tgv()
+        s.step(args.warmup)
+        torch.cuda.synchronize()
+        launches0 = s.lib.x3d_solver_launches_per_step(s.h)
+        if ws > 1:
+            torch.distributed.barrier()
+        with Clocks(local) as clk:
+            secs = time_steps(torch, s, args.steps, stream)
+        if ws > 1:
+            t = torch.tensor([secs], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            secs = t.item()
+        res[prec] = {"secs": secs, "clocks": clk.summary(), "launches": launches0}
+        solvers[prec] = s
+    # kinetic energy of both solvers after the same number of steps
+    if len(solvers) == 2:
+        for prec, s in solvers.items():
+            ke[prec] = float(s.tgv_stats()[0])
+    # e2e through the public API with host buffers: H2D velocity (pinned) ->
+    # one step -> D2H velocity, every step, on the mixed solver
+    e2e = None
+    s = solvers.get("mixed") or solvers[list(solvers)[0]]
+    host = [torch.empty((n, n, n), dtype=torch.float64, pin_memory=True) for _ in range(3)]
+    dev = [torch.empty((n, n, n), dtype=torch.float64, device="cuda") for _ in range(3)]
+    for h, d in zip(host, dev):
+        h.fill_(0.1)
+    lib = s.lib
+    import ctypes
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    e2e_steps = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for h, d in zip(host, dev):
+            d.copy_(h, non_blocking=True)
+        lib.x3d_solver_set_velocity(s.h, ptr(dev[0]), ptr(dev[1]), ptr(dev[2]), 1)
+        s.step(1)
+        lib.x3d_solver_get_velocity(s.h, ptr(dev[0]), ptr(dev[1]), ptr(dev[2]), 1)
+        for h, d in zip(host, dev):
+            h.copy_(d, non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_secs = (time.perf_counter() - t0) / e2e_steps
+    e2e = {"value": round(N / e2e_secs / 1e6 * ws, 3), "unit": UNIT, "h2d_bytes_per_step": 3 * N * 8,
+           "d2h_bytes_per_step": 3 * N * 8}
+    del host, dev
+    # dominant kernel, timed alone with CUDA events: y-direction compact first
+    # derivative in FP32 on the 512^3 field (algorithmic bytes = (N_in+N_out)*4)
+    u32 = torch.randn((n, n, n), dtype=torch.float32, device="cuda")
+    o32 = torch.empty_like(u32)
+    ksec = time_kernel(torch, lambda: ctx.apply(1, x3d.OP_DER1, 0, u32, out=o32), 20, stream)
+    kbytes = 2 * N * 4
+    u64 = torch.randn((n, n, n), dtype=torch.float64, device="cuda")
+    o64 = torch.empty_like(u64)
+    ksec64 = time_kernel(torch, lambda: ctx.apply(1, x3d.OP_DER1, 0, u64, out=o64), 10, stream)
+    pk, pk_kind = peaks()
+    if rank != 0:
+        return
+    main = res.get("mixed") or res[list(res)[0]]
+    secs = main["secs"]
+    value = N * args.steps * ws / secs / 1e6
+    cpu_rate, cpu_threads, _ = cpu_oracle_rate(args.cpu_n, 1) if not args.no_cpu else (None, 0, 0)
+    achieved = kbytes / ksec / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * secs / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "mixed f32/f64" if "mixed" in res else "f64",
+        "data": "synthetic",
+        "config": {"workload": "tgv_512^3_ab3" if n == 512 else "tgv_%d^3_ab3" % n, "grid": [n, n, n],
+                   "re": 1600, "dt": dt, "time_scheme": "AB3", "l2": "inputs larger than L2 (fields %.2f GB)"
+                   % (N * 8 / 1e9), "parallelism": "replicas" if ws > 1 else "1gpu"},
+        "clocks": main["clocks"],
+        "e2e": e2e,
+        "gpu_launches": int(main["launches"] * args.steps),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk, "unit": "GB/s",
+                     "frac": round(achieved / pk, 4), "traffic": None,
+                     "kernel": "line_kernel<float,DER1> y-lines 512^3 (dery FP32)",
+                     "peak_source": pk_kind},
+        "cpu_baseline": {"value": round(cpu_rate, 4) if cpu_rate else None, "unit": UNIT, "cores": cpu_threads,
+                         "kind": "port",
+                         "sample": "oracle TGV %d^3, 1 AB3 step, rate per grid point" % args.cpu_n},
+    }
+    if "fp64" in res:
+        f = res["fp64"]
+        line["fp64"] = {"value": round(N * args.steps * ws / f["secs"] / 1e6, 3),
+                        "ms_per_step": round(1e3 * f["secs"] / args.steps, 3), "clocks": f["clocks"],
+                        "dery_f64_gbs": round(2 * N * 8 / ksec64 / 1e9, 1)}
+    if ke:
+        line["ke_mixed_minus_fp64"] = ke["mixed"] - ke["fp64"]
+        line["ke_fp64"] = ke["fp64"]
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"])
+    ap.add_argument("--cpu-n", type=int, default=64)
+    ap.add_argument("--ref-n", type=int, default=128)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,257 @@
+/*
+ * x3d_gpu.h -- C ABI of libx3dgpu.so, the GB300 (sm_103a) implementation of
+ * Xcompact3d's per-timestep hot path.
+ *
+ * Every entry point mirrors one reference routine: the same name (prefixed
+ * x3d_), the same argument order and meaning, and the same array layout
+ * (Fortran column-major, x fastest).  Differences from the Fortran interface,
+ * all deliberate:
+ *   - a context handle comes first; it owns the grid, the numerical options,
+ *     and the coefficient tables already resident in device memory;
+ *   - field arguments (t, u) are DEVICE pointers; the work arrays r and s that
+ *     the Fortran interface passes are accepted and ignored (may be NULL): the
+ *     Sherman-Morrison vector is data-independent and lives in the context;
+ *   - coefficient-vector arguments (ff, fs, fw, ...) are HOST pointers to the
+ *     caller's copies (as a Fortran caller has them) or NULL.  When given, they
+ *     must match one of the context's coefficient sets bit for bit, otherwise
+ *     the call returns X3D_ERR_COEF; NULL selects the set the reference's
+ *     callers use for that parity (npaire=1 -> the "p" set);
+ *   - the trailing `stream` is a cudaStream_t (NULL = legacy default stream);
+ *     every call is stream-ordered and asynchronous;
+ *   - every call returns an int status (X3D_OK or a negative X3D_ERR_*)
+ *     instead of aborting.
+ * Thread safety: one context per host thread; no global mutable state.
+ *
+ * The _f32 variants are the single-precision build of the same routine
+ * (reference built without -DDOUBLE_PREC): float fields, float coefficients.
+ */
+#ifndef X3D_GPU_H
+#define X3D_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  X3D_OK = 0,
+  X3D_ERR_ARG = -1,         /* NULL handle/pointer or invalid enum value      */
+  X3D_ERR_SHAPE = -2,       /* dims do not match the context's grid           */
+  X3D_ERR_BC = -3,          /* unsupported boundary-condition / parity combo  */
+  X3D_ERR_DTYPE = -4,       /* precision not available for this routine       */
+  X3D_ERR_CUDA = -5,        /* a CUDA runtime call failed                     */
+  X3D_ERR_COEF = -6,        /* coefficient vectors match no context set       */
+  X3D_ERR_UNSUPPORTED = -7, /* option outside the implemented scope           */
+  X3D_ERR_NOMEM = -8,       /* device allocation failed                       */
+  X3D_ERR_STATE = -9        /* solver not initialised / numerical blow-up     */
+};
+
+typedef struct x3d_ctx x3d_ctx;
+typedef struct x3d_solver x3d_solver;
+
+/* Grid: the BasicParam namelist subset (src/parameters.f90:45-90).
+ * ncl: 0 periodic, 1 free-slip, 2 Dirichlet. */
+typedef struct {
+  int nx, ny, nz;
+  double xlx, yly, zlz;
+  int nclx1, nclxn, ncly1, nclyn, nclz1, nclzn;
+  int istret;  /* mesh stretching in y; only 0 is implemented */
+  double beta;
+} x3d_grid;
+
+/* Numerical options: NumOptions subset (src/parameters.f90; defaults in
+ * parameter_defaults). */
+typedef struct {
+  int ifirstder;       /* 1 or 4 (6th-order compact)                       */
+  int isecondder;      /* 1, 4 or 5 (hyperviscous)                         */
+  int ipinter;         /* 1, 2 or 3                                        */
+  double filter_alpha; /* alpha_f of the compact filter (fpi2 / C_filter)  */
+  double nu0nu, cnu;   /* hyperviscous parameters (isecondder=5)           */
+} x3d_numopts;
+
+/* --- context --------------------------------------------------------------
+ * Replaces init-time setup: schemes() (src/schemes.f90:7-409), filter()
+ * (src/filters.f90:5-59) and decomp_2d_poisson_init (src/poisson.f90:73-255).
+ * Selects the current CUDA device's tables; all later calls must run on that
+ * device. */
+int x3d_ctx_create(const x3d_grid* grid, const x3d_numopts* opts, x3d_ctx** out);
+int x3d_ctx_destroy(x3d_ctx* ctx);
+const char* x3d_strerror(int status);
+
+/* Host copy of a coefficient vector, so a Fortran or C caller can pass the
+ * same arrays the reference passes.  axis 0..2; `which` uses the numbering of
+ * X3D_COEF_* below; returns the vector length or a negative status. */
+enum {
+  X3D_COEF_FF = 0, X3D_COEF_FS, X3D_COEF_FW, X3D_COEF_FFP, X3D_COEF_FSP, X3D_COEF_FWP,
+  X3D_COEF_SF, X3D_COEF_SS, X3D_COEF_SW, X3D_COEF_SFP, X3D_COEF_SSP, X3D_COEF_SWP,
+  X3D_COEF_FIFF, X3D_COEF_FIFS, X3D_COEF_FIFW, X3D_COEF_FIFFP, X3D_COEF_FIFSP, X3D_COEF_FIFWP,
+  X3D_COEF_CF6, X3D_COEF_CS6, X3D_COEF_CW6,
+  X3D_COEF_CIF6, X3D_COEF_CIS6, X3D_COEF_CIW6,
+  X3D_COEF_CIFP6, X3D_COEF_CISP6, X3D_COEF_CIWP6,
+  X3D_COEF_CFIP6, X3D_COEF_CSIP6, X3D_COEF_CWIP6,
+  X3D_COEF_CIFIP6, X3D_COEF_CISIP6, X3D_COEF_CIWIP6,
+  X3D_COEF_CFI6, X3D_COEF_CSI6, X3D_COEF_CWI6,
+  X3D_COEF_CIFI6, X3D_COEF_CISI6, X3D_COEF_CIWI6,
+  X3D_COEF_CFP6, X3D_COEF_CSP6, X3D_COEF_CWP6,
+  X3D_COEF_COUNT
+};
+int x3d_get_coeffs(const x3d_ctx* ctx, int axis, int which, double* out, int capacity);
+
+/* --- compact first/second derivatives --------------------------------------
+ * DERIVATIVE_X / _Y / _YY / _Z interfaces, src/module_param.f90:135-170;
+ * implementations src/derive.f90:7-3792 (derx_00 ... derzz_22, bound by BC in
+ * src/schemes.f90:30-64).  lind is used by the reference only for IBM and is
+ * ignored.  ppy (dery only) is applied when the grid is stretched. */
+int x3d_derx(x3d_ctx* ctx, double* tx, const double* ux, double* rx, double* sx, const double* ffx,
+             const double* fsx, const double* fwx, int nx, int ny, int nz, int npaire, double lind,
+             void* stream);
+int x3d_dery(x3d_ctx* ctx, double* ty, const double* uy, double* ry, double* sy, const double* ffy,
+             const double* fsy, const double* fwy, const double* ppy, int nx, int ny, int nz, int npaire,
+             double lind, void* stream);
+int x3d_derz(x3d_ctx* ctx, double* tz, const double* uz, double* rz, double* sz, const double* ffz,
+             const double* fsz, const double* fwz, int nx, int ny, int nz, int npaire, double lind,
+             void* stream);
+int x3d_derxx(x3d_ctx* ctx, double* tx, const double* ux, double* rx, double* sx, const double* sfx,
+              const double* ssx, const double* swx, int nx, int ny, int nz, int npaire, double lind,
+              void* stream);
+int x3d_deryy(x3d_ctx* ctx, double* ty, const double* uy, double* ry, double* sy, const double* sfy,
+              const double* ssy, const double* swy, int nx, int ny, int nz, int npaire, double lind,
+              void* stream);
+int x3d_derzz(x3d_ctx* ctx, double* tz, const double* uz, double* rz, double* sz, const double* sfz,
+              const double* ssz, const double* swz, int nx, int ny, int nz, int npaire, double lind,
+              void* stream);
+
+/* --- compact filters --------------------------------------------------------
+ * FILTER_X / _Y / _Z interfaces, src/module_param.f90:202-226; implementations
+ * src/filters.f90:221-1377 (filx_00 ... filz_22). */
+int x3d_filx(x3d_ctx* ctx, double* tx, const double* ux, double* rx, double* fisx, const double* fiffx,
+             const double* fifsx, const double* fifwx, int nx, int ny, int nz, int npaire, double lind,
+             void* stream);
+int x3d_fily(x3d_ctx* ctx, double* ty, const double* uy, double* ry, double* fisy, const double* fiffy,
+             const double* fifsy, const double* fifwy, int nx, int ny, int nz, int npaire, double lind,
+             void* stream);
+int x3d_filz(x3d_ctx* ctx, double* tz, const double* uz, double* rz, double* fisz, const double* fiffz,
+             const double* fifsz, const double* fifwz, int nx, int ny, int nz, int npaire, double lind,
+             void* stream);
+
+/* --- staggered (velocity <-> pressure mesh) operators -------------------------
+ * src/derive.f90:3796-5615.  Argument lists follow the Fortran subroutines. */
+int x3d_derxvp(x3d_ctx* ctx, double* tx, const double* ux, double* rx, double* sx, const double* cfx6,
+               const double* csx6, const double* cwx6, int nx, int nxm, int ny, int nz, int npaire,
+               void* stream);
+int x3d_interxvp(x3d_ctx* ctx, double* tx, const double* ux, double* rx, double* sx, const double* cifx6,
+                 const double* cisx6, const double* ciwx6, int nx, int nxm, int ny, int nz, int npaire,
+                 void* stream);
+int x3d_derxpv(x3d_ctx* ctx, double* tx, const double* ux, double* rx, double* sx, const double* cfi6,
+               const double* csi6, const double* cwi6, const double* cfx6, const double* csx6,
+               const double* cwx6, int nxm, int nx, int ny, int nz, int npaire, void* stream);
+int x3d_interxpv(x3d_ctx* ctx, double* tx, const double* ux, double* rx, double* sx, const double* cifi6,
+                 const double* cisi6, const double* ciwi6, const double* cifx6, const double* cisx6,
+                 const double* ciwx6, int nxm, int nx, int ny, int nz, int npaire, void* stream);
+int x3d_interyvp(x3d_ctx* ctx, double* ty, const double* uy, double* ry, double* sy, const double* cify6,
+                 const double* cisy6, const double* ciwy6, int nx, int ny, int nym, int nz, int npaire,
+                 void* stream);
+int x3d_deryvp(x3d_ctx* ctx, double* ty, const double* uy, double* ry, double* sy, const double* cfy6,
+               const double* csy6, const double* cwy6, const double* ppyi, int nx, int ny, int nym, int nz,
+               int npaire, void* stream);
+int x3d_interypv(x3d_ctx* ctx, double* ty, const double* uy, double* ry, double* sy, const double* cifi6y,
+                 const double* cisi6y, const double* ciwi6y, const double* cify6, const double* cisy6,
+                 const double* ciwy6, int nx, int nym, int ny, int nz, int npaire, void* stream);
+int x3d_derypv(x3d_ctx* ctx, double* ty, const double* uy, double* ry, double* sy, const double* cfi6y,
+               const double* csi6y, const double* cwi6y, const double* cfy6, const double* csy6,
+               const double* cwy6, const double* ppy, int nx, int nym, int ny, int nz, int npaire,
+               void* stream);
+int x3d_derzvp(x3d_ctx* ctx, double* tz, const double* uz, double* rz, double* sz, const double* cfz6,
+               const double* csz6, const double* cwz6, int nx, int ny, int nz, int nzm, int npaire,
+               void* stream);
+int x3d_interzvp(x3d_ctx* ctx, double* tz, const double* uz, double* rz, double* sz, const double* cifz6,
+                 const double* cisz6, const double* ciwz6, int nx, int ny, int nz, int nzm, int npaire,
+                 void* stream);
+int x3d_derzpv(x3d_ctx* ctx, double* tz, const double* uz, double* rz, double* sz, const double* cfiz6,
+               const double* csiz6, const double* cwiz6, const double* cfz6, const double* csz6,
+               const double* cwz6, int nx, int ny, int nzm, int nz, int npaire, void* stream);
+int x3d_interzpv(x3d_ctx* ctx, double* tz, const double* uz, double* rz, double* sz, const double* cifiz6,
+                 const double* cisiz6, const double* ciwiz6, const double* cifz6, const double* cisz6,
+                 const double* ciwz6, int nx, int ny, int nzm, int nz, int npaire, void* stream);
+
+/* --- generic operator entry (used by the per-routine wrappers above) --------
+ * op: 0 der1, 1 der2, 2 filter, 3 d(v->p), 4 interp(v->p), 5 d(p->v),
+ * 6 interp(p->v).  axis 0..2.  dims_in = extents of u (nx_in, ny_in, nz_in).
+ * dtype: 0 = float64, 1 = float32.  coefset: -1 = default for npaire,
+ * 0 = plain set, 1 = "p" set. */
+int x3d_apply(x3d_ctx* ctx, int axis, int op, int npaire, int coefset, int dtype, void* t, const void* u,
+              const int* dims_in, void* stream);
+
+/* --- single-precision builds of the derivative / filter routines ---------- */
+int x3d_derx_f32(x3d_ctx* ctx, float* tx, const float* ux, int nx, int ny, int nz, int npaire, void* stream);
+int x3d_dery_f32(x3d_ctx* ctx, float* ty, const float* uy, int nx, int ny, int nz, int npaire, void* stream);
+int x3d_derz_f32(x3d_ctx* ctx, float* tz, const float* uz, int nx, int ny, int nz, int npaire, void* stream);
+int x3d_derxx_f32(x3d_ctx* ctx, float* tx, const float* ux, int nx, int ny, int nz, int npaire, void* stream);
+int x3d_deryy_f32(x3d_ctx* ctx, float* ty, const float* uy, int nx, int ny, int nz, int npaire, void* stream);
+int x3d_derzz_f32(x3d_ctx* ctx, float* tz, const float* uz, int nx, int ny, int nz, int npaire, void* stream);
+int x3d_filx_f32(x3d_ctx* ctx, float* tx, const float* ux, int nx, int ny, int nz, int npaire, void* stream);
+int x3d_fily_f32(x3d_ctx* ctx, float* ty, const float* uy, int nx, int ny, int nz, int npaire, void* stream);
+int x3d_filz_f32(x3d_ctx* ctx, float* tz, const float* uz, int nx, int ny, int nz, int npaire, void* stream);
+
+/* --- Poisson solve ------------------------------------------------------------
+ * poisson(rhs) procedure pointer, src/poisson.f90:57-62; all-periodic solver
+ * poisson_000, src/poisson.f90:298-410.  rhs (nxm,nym,nzm) in device memory is
+ * overwritten by the solution.  precision: 0 = FP64 FFT, 1 = FP32 FFT. */
+int x3d_poisson(x3d_ctx* ctx, double* rhs, void* stream);
+int x3d_poisson_ex(x3d_ctx* ctx, double* rhs, int precision, void* stream);
+
+/* --- 2DECOMP transposes ------------------------------------------------------
+ * transpose_x_to_y / y_to_z / z_to_y / y_to_x of 2DECOMP&FFT.  On one GPU the
+ * X-, Y- and Z-pencils are the same (nx,ny,nz) array, so each is a device copy
+ * (or nothing when src == dst).  n = number of elements. */
+int x3d_transpose_x_to_y(x3d_ctx* ctx, const double* src, double* dst, long long n, void* stream);
+int x3d_transpose_y_to_z(x3d_ctx* ctx, const double* src, double* dst, long long n, void* stream);
+int x3d_transpose_z_to_y(x3d_ctx* ctx, const double* src, double* dst, long long n, void* stream);
+int x3d_transpose_y_to_x(x3d_ctx* ctx, const double* src, double* dst, long long n, void* stream);
+
+/* --- projection pieces ---------------------------------------------------------
+ * divergence (nlock=1, src/navier.f90:257-372), gradp (src/navier.f90:386-499),
+ * cor_vel (src/navier.f90:206-249).  Device pointers; pp3 is (nxm,nym,nzm). */
+int x3d_divergence(x3d_ctx* ctx, double* pp3, const double* ux, const double* uy, const double* uz,
+                   void* stream);
+int x3d_gradp(x3d_ctx* ctx, double* px, double* py, double* pz, const double* pp3, void* stream);
+int x3d_cor_vel(x3d_ctx* ctx, double* ux, double* uy, double* uz, const double* px, const double* py,
+                const double* pz, void* stream);
+
+/* --- incompressible solver (the time loop body of src/xcompact3d.f90:29-102)
+ * for the plain periodic case: calculate_transeq_rhs (src/transeq.f90:20-591),
+ * int_time (src/time_integrators.f90), solve_poisson + cor_vel
+ * (src/navier.f90).  The solver owns u, v, w, the time-integrator history and
+ * the work fields, all resident in device memory.
+ * precision: X3D_PREC_FP64 computes everything in binary64;
+ * X3D_PREC_MIXED runs derivatives, convective/viscous terms and the staggered
+ * operators in binary32, keeps the velocity, the time-integrator history and
+ * accumulation, and the Poisson solve in binary64. */
+enum { X3D_PREC_FP64 = 0, X3D_PREC_MIXED = 1 };
+typedef struct {
+  int itimescheme; /* 3 = AB3 (Euler, AB2 start-up), 5 = RK3 */
+  double dt;
+  double xnu;      /* 1/Re */
+  int precision;   /* X3D_PREC_* */
+} x3d_solver_opts;
+
+int x3d_solver_create(x3d_ctx* ctx, const x3d_solver_opts* opts, x3d_solver** out);
+int x3d_solver_destroy(x3d_solver* s);
+/* Copy the velocity in or out.  on_device: 1 = device pointers, 0 = host. */
+int x3d_solver_set_velocity(x3d_solver* s, const double* ux, const double* uy, const double* uz, int on_device);
+int x3d_solver_get_velocity(x3d_solver* s, double* ux, double* uy, double* uz, int on_device);
+/* Initial condition of init_tgv (src/Case-TGV.f90:25-107), iin=1. */
+int x3d_solver_init_tgv(x3d_solver* s);
+/* Advance nsteps time steps (each with its sub-steps), stream-ordered. */
+int x3d_solver_step(x3d_solver* s, int nsteps, void* stream);
+/* TGV statistics of postprocess_tgv (src/Case-TGV.f90:189-477):
+ * out = {E_k, eps (strain), eps2 (laplacian), enstrophy}.  Synchronises. */
+int x3d_solver_tgv_stats(x3d_solver* s, double* out, void* stream);
+/* max |div u| on the pressure mesh (test_flow / divergence nlock=2).  Synchronises. */
+int x3d_solver_divmax(x3d_solver* s, double* out, void* stream);
+/* Number of kernels this solver launches per time step. */
+int x3d_solver_launches_per_step(x3d_solver* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* X3D_GPU_H */

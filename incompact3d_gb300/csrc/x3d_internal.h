@@ -1,0 +1,132 @@
+// Internal declarations shared by the libx3dgpu translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "x3d_gpu.h"
+
+namespace x3d {
+
+typedef std::vector<double> dvec;
+
+// Operator kinds: one generic "banded right-hand side + tridiagonal solve
+// (+ periodic Sherman-Morrison)" kernel covers all of them.
+enum OpKind { K_DER1 = 0, K_DER2 = 1, K_FIL = 2, K_DVP = 3, K_IVP = 4, K_DPV = 5, K_IPV = 6, K_COUNT = 7 };
+
+constexpr int kMaxTerms = 6;   // terms in one boundary-row expression
+constexpr int kMaxEnt = 4;     // signed samples inside one term
+constexpr int kMaxBRows = 10;  // boundary rows per operator (both ends)
+
+// One boundary row:  t[row] = sum_t coef[t] * (sum_e mult[t][e] * u[idx[t][e]])
+// evaluated left to right, exactly the way the reference writes the row.
+struct BRow {
+  int row = 0;
+  int nterms = 0;
+  double coef[kMaxTerms] = {0};
+  int nent[kMaxTerms] = {0};
+  int idx[kMaxTerms][kMaxEnt] = {{0}};
+  int mult[kMaxTerms][kMaxEnt] = {{0}};
+};
+
+// Per-axis coefficients: the restatement of the reference's init-time
+// coefficient computation (src/schemes.f90, src/filters.f90).
+struct AxisCoef {
+  int n = 0, nm = 0, ncl1 = 0, ncln = 0;
+  bool periodic = true;
+  double len = 0, d = 0, d2 = 0;
+  // first derivative
+  double alfai, afi, bfi, af1, bf1, cf1, af2, afm, afn, bfn, cfn, alfa1, alfa2, alfam, alfan;
+  // second derivative
+  double alsai, asi, bsi, csi, dsi, as1, bs1, cs1, ds1, as2, as3, bs3, as4, bs4, cs4, asn, bsn, csn, dsn, asm_,
+      ast, bst, astt, bstt, cstt;
+  // staggered
+  double alcai6, aci6, bci6, ailcai6, aici6, bici6, cici6s, dici6;
+  // filter
+  double fiali, fiai, fibi, fici, fidi, fia2, fib2, fic2, fid2, fia3, fib3, fic3, fid3, fie3, fif3, fiam, fibm,
+      ficm, fidm, fiap, fibp, ficp, fidp, fiep, fifp;
+  // coefficient vectors, indexed by X3D_COEF_*
+  dvec vecs[X3D_COEF_COUNT];
+};
+
+// Plan of one operator (axis, kind, npaire, coefficient set): everything the
+// generic line kernel needs, on host and in device memory.
+struct OpPlan {
+  int axis = 0, kind = 0, npaire = 0, coefset = 0;
+  int nin = 0, nout = 0;
+  bool periodic = false;
+  double ca = 0, cb = 0, cc = 0, cd = 0;  // interior stencil coefficients
+  double alpha = 0, den = 1;              // Sherman-Morrison
+  int nbrows = 0;
+  BRow brows[kMaxBRows];
+  dvec s, f, w, rsm;  // Thomas factors and the precomputed SM vector
+  int L = 0;          // chunk length the fix-up factors below were built for
+  dvec pf, qb;        // chunked-solve fix-up factors
+  // device copies: [s | f | w | pf | qb | rsm] x nout, in f64 and f32
+  double* dev64 = nullptr;
+  float* dev32 = nullptr;
+};
+
+struct Ctx;
+
+// Build all per-axis coefficients (host).  Returns X3D_OK or an error.
+int build_axis(AxisCoef& a, int n, double len, int ncl1, int ncln, const x3d_numopts& o);
+// Build the plan of one operator (host part).  Returns X3D_OK or an error.
+int build_plan(const AxisCoef& a, int axis, int kind, int npaire, int coefset, OpPlan& p);
+// Default coefficient set for (kind, npaire) as the reference's callers pick it.
+int default_coefset(int kind, int npaire);
+// Index (X3D_COEF_*) of the (f, s, w) vectors of a plan's coefficient set.
+void coef_indices(const AxisCoef& a, int kind, int coefset, int* fi, int* si, int* wi);
+
+// Poisson tables (periodic): modified wavenumber^2 and interpolation transfer.
+void waves_tables(const AxisCoef& a, dvec& k2, dvec& tr);
+
+// Device scratch owned by a context, grown on demand (used by the stand-alone
+// projection entry points, which have no solver to borrow work fields from).
+struct Workspace {
+  void* buf = nullptr;
+  size_t bytes = 0;
+  ~Workspace() {
+    if (buf) cudaFree(buf);
+  }
+};
+
+struct Ctx {
+  x3d_grid grid;
+  x3d_numopts opts;
+  int device = 0;
+  int num_sms = 0;
+  AxisCoef ax[3];
+  std::map<int, std::unique_ptr<OpPlan>> plans;  // key = packed (axis,kind,npaire,coefset)
+  // Poisson device tables
+  double* d_k2[3] = {nullptr, nullptr, nullptr};
+  double* d_tr[3] = {nullptr, nullptr, nullptr};
+  double* d_twid = nullptr;  // FFT twiddles (see x3d_fft.cu)
+  float* d_twid32 = nullptr;
+  int twid_n = 0;
+  void* fft_work = nullptr;  // complex spectrum buffer
+  size_t fft_work_bytes = 0;
+  std::unique_ptr<Workspace> ws;
+  ~Ctx();
+};
+
+// Device scratch of at least `bytes` bytes (contents undefined).
+int ctx_workspace(Ctx* c, size_t bytes, void** out);
+
+// Get (building on first use) the device plan of an operator.
+int get_plan(Ctx* c, int axis, int kind, int npaire, int coefset, OpPlan** out);
+
+// Launch the generic line kernel.  T = double or float.
+template <typename T>
+int launch_line_op(Ctx* c, OpPlan* p, T* out, const T* in, const int* dims_in, const T* pp, cudaStream_t st);
+
+// Poisson (periodic, all three directions).  precision 0: FP64 FFT, 1: FP32 FFT.
+int poisson_periodic(Ctx* c, double* rhs, int precision, cudaStream_t st);
+
+inline int cuda_status(cudaError_t e) { return e == cudaSuccess ? X3D_OK : X3D_ERR_CUDA; }
+
+}  // namespace x3d

@@ -1,0 +1,140 @@
+// Host launcher of the generic compact-operator line kernel
+// (x3d_line_kernel.cuh): per-operator plan finalisation (chunk fix-up
+// factors, device upload) and argument marshalling.
+#include "x3d_line_kernel.cuh"
+
+namespace x3d {
+
+using namespace lk;
+
+namespace {
+
+template <typename T>
+int dispatch(const LineArgs<T>& a, int kind, bool xl, int lmax, dim3 grid, size_t smem, cudaStream_t st) {
+  switch (kind) {
+    case K_DER1: return line_dispatch<K_DER1>(a, xl, lmax, grid, smem, st);
+    case K_DER2: return line_dispatch<K_DER2>(a, xl, lmax, grid, smem, st);
+    case K_FIL: return line_dispatch<K_FIL>(a, xl, lmax, grid, smem, st);
+    case K_DVP: return line_dispatch<K_DVP>(a, xl, lmax, grid, smem, st);
+    case K_IVP: return line_dispatch<K_IVP>(a, xl, lmax, grid, smem, st);
+    case K_DPV: return line_dispatch<K_DPV>(a, xl, lmax, grid, smem, st);
+    case K_IPV: return line_dispatch<K_IPV>(a, xl, lmax, grid, smem, st);
+  }
+  return X3D_ERR_ARG;
+}
+
+template <typename T>
+const T* plan_dev(const OpPlan* p);
+template <>
+const double* plan_dev<double>(const OpPlan* p) { return p->dev64; }
+template <>
+const float* plan_dev<float>(const OpPlan* p) { return p->dev32; }
+
+}  // namespace
+
+// Chunk length and fix-up factors for a plan (host), plus device upload.
+int finalize_plan(OpPlan* p) {
+  const int n = p->nout;
+  const int L = (n + CHUNKS - 1) / CHUNKS;
+  if (L > 32) return X3D_ERR_UNSUPPORTED;  // lines longer than 512 points
+  p->L = L;
+  p->pf.assign(n, 0.0);
+  p->qb.assign(n, 0.0);
+  for (int c = 0; c * L < n; ++c) {
+    const int s0 = c * L, e0 = std::min(s0 + L, n) - 1;
+    double acc = 1.0;
+    for (int r = s0; r <= e0; ++r) {
+      acc = acc * (-p->s[r]);
+      p->pf[r] = acc;
+    }
+    acc = 1.0;
+    for (int r = e0; r >= s0; --r) {
+      acc = acc * (-(p->f[r] * p->w[r]));
+      p->qb[r] = acc;
+    }
+  }
+  std::vector<double> h64(6 * (size_t)n);
+  std::vector<float> h32(6 * (size_t)n);
+  const dvec* parts[6] = {&p->s, &p->f, &p->w, &p->pf, &p->qb, &p->rsm};
+  for (int q = 0; q < 6; ++q)
+    for (int r = 0; r < n; ++r) {
+      h64[(size_t)q * n + r] = (*parts[q])[r];
+      h32[(size_t)q * n + r] = (float)(*parts[q])[r];
+    }
+  if (cudaMalloc(&p->dev64, h64.size() * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
+  if (cudaMalloc(&p->dev32, h32.size() * sizeof(float)) != cudaSuccess) return X3D_ERR_NOMEM;
+  if (cudaMemcpy(p->dev64, h64.data(), h64.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+    return X3D_ERR_CUDA;
+  if (cudaMemcpy(p->dev32, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+    return X3D_ERR_CUDA;
+  return X3D_OK;
+}
+
+template <typename T>
+int launch_line_op(Ctx* c, OpPlan* p, T* out, const T* in, const int* dims_in, const T* pp, cudaStream_t st) {
+  (void)c;
+  if (!out || !in) return X3D_ERR_ARG;
+  if (dims_in[p->axis] != p->nin) return X3D_ERR_SHAPE;
+  LineArgs<T> a;
+  std::memset(&a, 0, sizeof(a));
+  a.in = in;
+  a.out = out;
+  a.nin = p->nin;
+  a.nout = p->nout;
+  a.L = p->L;
+  const long long nx = dims_in[0], ny = dims_in[1], nz = dims_in[2];
+  dim3 grid;
+  const bool xl = (p->axis == 0);
+  if (p->axis == 0) {
+    a.na = (int)ny;
+    a.sa_in = p->nin; a.sb_in = ny * p->nin; a.rs_in = 1;
+    a.sa_out = p->nout; a.sb_out = ny * p->nout; a.rs_out = 1;
+    grid = dim3((unsigned)((ny + LANES - 1) / LANES), (unsigned)nz);
+  } else if (p->axis == 1) {
+    a.na = (int)nx;
+    a.sa_in = 1; a.sb_in = nx * p->nin; a.rs_in = nx;
+    a.sa_out = 1; a.sb_out = nx * p->nout; a.rs_out = nx;
+    grid = dim3((unsigned)((nx + LANES - 1) / LANES), (unsigned)nz);
+  } else {
+    a.na = (int)nx;
+    a.sa_in = 1; a.sb_in = nx; a.rs_in = nx * ny;
+    a.sa_out = 1; a.sb_out = nx; a.rs_out = nx * ny;
+    grid = dim3((unsigned)((nx + LANES - 1) / LANES), (unsigned)ny);
+  }
+  if (grid.y > 65535) return X3D_ERR_UNSUPPORTED;
+  const T* dv = plan_dev<T>(p);
+  const int n = p->nout;
+  a.s = dv; a.f = dv + n; a.w = dv + 2 * n; a.pf = dv + 3 * n; a.qb = dv + 4 * n; a.rsm = dv + 5 * n;
+  a.pp = pp;
+  a.ca = (T)p->ca; a.cb = (T)p->cb; a.cc = (T)p->cc; a.cd = (T)p->cd;
+  a.alpha = (T)p->alpha;
+  a.den = (T)p->den;
+  a.periodic = p->periodic ? 1 : 0;
+  a.nterms_int = 4;
+  if (p->kind == K_DER2 && p->cc == 0.0 && p->cd == 0.0) a.nterms_int = 2;
+  if ((p->kind == K_IVP || p->kind == K_IPV) && p->cd == 0.0) a.nterms_int = 3;
+  a.nbrows = p->nbrows;
+  for (int q = 0; q < p->nbrows; ++q) {
+    const BRow& s = p->brows[q];
+    BRowD<T>& d = a.brows[q];
+    d.row = (short)s.row;
+    d.nterms = (signed char)s.nterms;
+    for (int t = 0; t < kMaxTerms; ++t) {
+      d.coef[t] = (T)s.coef[t];
+      d.nent[t] = (signed char)s.nent[t];
+      for (int e = 0; e < kMaxEnt; ++e) {
+        d.idx[t][e] = (short)s.idx[t][e];
+        d.mult[t][e] = (signed char)s.mult[t][e];
+      }
+    }
+  }
+  const int lmax = (p->L <= 8) ? 8 : 32;
+  const size_t smem = line_smem<T>(p->nin, p->nout);
+  if (smem > 227 * 1024) return X3D_ERR_UNSUPPORTED;
+  return dispatch<T>(a, p->kind, xl, lmax, grid, smem, st);
+}
+
+template int launch_line_op<double>(Ctx*, OpPlan*, double*, const double*, const int*, const double*, cudaStream_t);
+template int launch_line_op<float>(Ctx*, OpPlan*, float*, const float*, const int*, const float*, cudaStream_t);
+
+}  // namespace x3d

@@ -1,0 +1,16 @@
+// Instantiations of the line kernel for one operator kind (K_IVP); split
+// out so the kernel variants compile in parallel.
+#include "x3d_line_kernel.cuh"
+
+namespace x3d {
+namespace lk {
+template <>
+int line_dispatch<K_IVP>(const LineArgs<double>& a, bool xl, int lmax, dim3 grid, size_t smem, cudaStream_t st) {
+  return dispatch_xl<double, K_IVP>(a, xl, lmax, grid, smem, st);
+}
+template <>
+int line_dispatch<K_IVP>(const LineArgs<float>& a, bool xl, int lmax, dim3 grid, size_t smem, cudaStream_t st) {
+  return dispatch_xl<float, K_IVP>(a, xl, lmax, grid, smem, st);
+}
+}  // namespace lk
+}  // namespace x3d

@@ -1,0 +1,699 @@
+// Incompressible time step for the plain periodic case, resident in HBM:
+//   calculate_transeq_rhs -> intt -> divergence -> poisson -> gradp -> cor_vel
+// (src/xcompact3d.f90:29-102, src/transeq.f90:73-591,
+//  src/time_integrators.f90:18-187, src/navier.f90:27-499), plus the TGV
+// statistics of postprocess_tgv (src/Case-TGV.f90:189-477).
+//
+// The 2DECOMP transposes between stages are identities on one GPU (X-, Y- and
+// Z-pencils are the same (nx,ny,nz) array), so the stages read the x-pencil
+// fields directly.  Time-integrator history is rotated by pointer, never copied.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <type_traits>
+#include <vector>
+
+#include "x3d_internal.h"
+
+namespace x3d {
+
+// ---------------------------------------------------------------------------
+// Pointwise kernels (grid-stride, 3 components per thread)
+// ---------------------------------------------------------------------------
+namespace {
+
+inline unsigned pw_blocks(Ctx* c, long long n) {
+  const long long per = 256LL * 4;
+  long long b = (n + per - 1) / per;
+  const long long cap = (long long)c->num_sms * 8;
+  if (b > cap) b = cap;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+#define GRID_STRIDE(i, n) \
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (n); i += (long long)gridDim.x * blockDim.x)
+
+// o_k = x_k * y
+template <typename T>
+__global__ void k_prod3(T* o1, T* o2, T* o3, const T* x1, const T* x2, const T* x3, const T* y, long long n) {
+  GRID_STRIDE(i, n) {
+    const T yy = y[i];
+    o1[i] = x1[i] * yy;
+    o2[i] = x2[i] * yy;
+    o3[i] = x3[i] * yy;
+  }
+}
+
+// o_k = a_k + y * b_k
+template <typename T>
+__global__ void k_addmul3(T* o1, T* o2, T* o3, const T* a1, const T* a2, const T* a3, const T* b1, const T* b2,
+                          const T* b3, const T* y, long long n) {
+  GRID_STRIDE(i, n) {
+    const T yy = y[i];
+    o1[i] = a1[i] + yy * b1[i];
+    o2[i] = a2[i] + yy * b2[i];
+    o3[i] = a3[i] + yy * b3[i];
+  }
+}
+
+// o_k = s1 * a_k + s2 * b_k
+template <typename T>
+__global__ void k_lin3(T* o1, T* o2, T* o3, const T* a1, const T* a2, const T* a3, const T* b1, const T* b2,
+                       const T* b3, T s1, T s2, long long n) {
+  GRID_STRIDE(i, n) {
+    o1[i] = s1 * a1[i] + s2 * b1[i];
+    o2[i] = s1 * a2[i] + s2 * b2[i];
+    o3[i] = s1 * a3[i] + s2 * b3[i];
+  }
+}
+
+// H_k = a_k - 0.5 * b_k + xnu * c_k  (final sum of momentum_rhs_eq; output may
+// be a different precision than the operands)
+template <typename T, typename H>
+__global__ void k_final3(H* o1, H* o2, H* o3, const T* a1, const T* a2, const T* a3, const T* b1, const T* b2,
+                         const T* b3, const T* c1, const T* c2, const T* c3, T xnu, long long n) {
+  GRID_STRIDE(i, n) {
+    o1[i] = (H)(a1[i] - T(0.5) * b1[i] + xnu * c1[i]);
+    o2[i] = (H)(a2[i] - T(0.5) * b2[i] + xnu * c2[i]);
+    o3[i] = (H)(a3[i] - T(0.5) * b3[i] + xnu * c3[i]);
+  }
+}
+
+// Adams-Bashforth / RK update of one component, in FP64:
+//   u = c1*h1 + c2*h2 + c3*h3 + u   (terms with a null pointer are skipped)
+// and, when u32 is non-null, an FP32 copy of the new u for the next operators.
+template <typename H>
+__global__ void k_intt(double* u, float* u32, const H* h1, const H* h2, const H* h3, double c1, double c2, double c3,
+                       long long n) {
+  GRID_STRIDE(i, n) {
+    double acc = c1 * (double)h1[i];
+    if (h2) acc = acc + c2 * (double)h2[i];
+    if (h3) acc = acc + c3 * (double)h3[i];
+    const double v = acc + u[i];
+    u[i] = v;
+    if (u32) u32[i] = (float)v;
+  }
+}
+
+template <typename T>
+__global__ void k_add(T* o, const T* a, const T* b, long long n) {
+  GRID_STRIDE(i, n) o[i] = a[i] + b[i];
+}
+
+template <typename T>
+__global__ void k_add_to64(double* o, const T* a, const T* b, long long n) {
+  GRID_STRIDE(i, n) o[i] = (double)(a[i] + b[i]);
+}
+
+__global__ void k_to32(float* o, const double* a, long long n) {
+  GRID_STRIDE(i, n) o[i] = (float)a[i];
+}
+
+// u -= px (cor_vel), FP64 state, optional FP32 copy
+template <typename T>
+__global__ void k_corvel(double* u1, double* u2, double* u3, float* v1, float* v2, float* v3, const T* p1,
+                         const T* p2, const T* p3, long long n) {
+  GRID_STRIDE(i, n) {
+    const double a = u1[i] - (double)p1[i];
+    const double b = u2[i] - (double)p2[i];
+    const double c = u3[i] - (double)p3[i];
+    u1[i] = a; u2[i] = b; u3[i] = c;
+    if (v1) { v1[i] = (float)a; v2[i] = (float)b; v3[i] = (float)c; }
+  }
+}
+
+__global__ void k_tgv_init(double* ux, double* uy, double* uz, int nx, int ny, int nz, double dx, double dy,
+                           double dz) {
+  const long long n = (long long)nx * ny * nz;
+  GRID_STRIDE(m, n) {
+    const int i = (int)(m % nx);
+    const int j = (int)((m / nx) % ny);
+    const int k = (int)(m / ((long long)nx * ny));
+    const double x = (double)i * dx, y = (double)j * dy, z = (double)k * dz;
+    ux[m] = sin(x) * cos(y) * cos(z);
+    uy[m] = -cos(x) * sin(y) * cos(z);
+    uz[m] = 0.0;
+  }
+}
+
+// Block partial sums for the TGV statistics; one value per block per quantity.
+// q: 0 = 0.5*sum(u^2+v^2+w^2); 1 = eps(strain); 2 = enstrophy; 3 = eps2
+__global__ void k_stats(const double* ux, const double* uy, const double* uz, const double* const* g,
+                        const double* const* l, double xnu, long long n, double* part) {
+  __shared__ double sh[4][256];
+  double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  GRID_STRIDE(m, n) {
+    const double u = ux[m], v = uy[m], w = uz[m];
+    a0 += 0.5 * (u * u + v * v + w * w);
+    // g: 0 du/dx 1 dv/dx 2 dw/dx 3 du/dy 4 dv/dy 5 dw/dy 6 du/dz 7 dv/dz 8 dw/dz
+    const double ta = g[0][m], tb = g[1][m], tc = g[2][m], td = g[3][m], te = g[4][m], tf = g[5][m], tg = g[6][m],
+                 th = g[7][m], ti = g[8][m];
+    const double s1 = 2.0 * ta, s2 = 2.0 * te, s3 = 2.0 * ti, s4 = td + tb, s5 = tg + tc, s6 = th + tf;
+    a1 += 0.5 * xnu * (s1 * s1 + s2 * s2 + s3 * s3 + 2.0 * (s4 * s4) + 2.0 * (s5 * s5) + 2.0 * (s6 * s6));
+    const double o1 = tf - th, o2 = tg - tc, o3 = tb - td;
+    a2 += 0.5 * (o1 * o1 + o2 * o2 + o3 * o3);
+    a3 += (-xnu) * (u * (l[0][m] + l[3][m] + l[6][m]) + v * (l[1][m] + l[4][m] + l[7][m]) +
+                    w * (l[2][m] + l[5][m] + l[8][m]));
+  }
+  sh[0][threadIdx.x] = a0; sh[1][threadIdx.x] = a1; sh[2][threadIdx.x] = a2; sh[3][threadIdx.x] = a3;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s)
+      for (int q = 0; q < 4; ++q) sh[q][threadIdx.x] += sh[q][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) part[(size_t)blockIdx.x * 4 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void k_absmax(const double* a, long long n, double* part) {
+  __shared__ double sh[256];
+  double m = 0;
+  GRID_STRIDE(i, n) m = fmax(m, fabs(a[i]));
+  sh[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Solver
+// ---------------------------------------------------------------------------
+struct SolverImpl {
+  Ctx* c = nullptr;
+  x3d_solver_opts o;
+  long long N = 0, Np = 0;  // velocity-mesh and pressure-mesh sizes
+  int itime = 0;            // completed steps
+  int ntime = 3, nsub = 1;
+  double adt[3] = {0, 0, 0}, bdt[3] = {0, 0, 0}, cdt[3] = {0, 0, 0}, gdt[3] = {0, 0, 0};
+  // FP64 state
+  double *ux = nullptr, *uy = nullptr, *uz = nullptr;
+  // operator-precision copies of the state (mixed only)
+  float *ux32 = nullptr, *uy32 = nullptr, *uz32 = nullptr;
+  // history: [component][slot], precision of the operators
+  void* H[3][3] = {{nullptr}};
+  // work fields in operator precision
+  void* W[16] = {nullptr};
+  void* P[8] = {nullptr};  // pressure-mesh / intermediate-mesh work
+  double* pp64 = nullptr;
+  double* part = nullptr;  // reduction partials
+  double* hpart = nullptr;
+  int launches = 0;
+  std::vector<void*> allocs;
+  ~SolverImpl() {
+    for (void* p : allocs) cudaFree(p);
+    if (hpart) cudaFreeHost(hpart);
+  }
+  template <typename T>
+  T* alloc(long long n) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, (size_t)n * sizeof(T)) != cudaSuccess) return nullptr;
+    allocs.push_back(p);
+    return (T*)p;
+  }
+  bool mixed() const { return o.precision == X3D_PREC_MIXED; }
+};
+
+}  // namespace x3d
+
+struct x3d_solver {
+  x3d::SolverImpl impl;
+};
+
+namespace x3d {
+
+template <typename T>
+static int op(SolverImpl* s, int axis, int kind, int npaire, T* out, const T* in, const int* dims, cudaStream_t st) {
+  OpPlan* p = nullptr;
+  int rc = get_plan(s->c, axis, kind, npaire, default_coefset(kind, npaire), &p);
+  if (rc != X3D_OK) return rc;
+  s->launches++;
+  return launch_line_op<T>(s->c, p, out, in, dims, nullptr, st);
+}
+
+#define RC(x)                      \
+  do {                             \
+    int _r = (x);                  \
+    if (_r != X3D_OK) return _r;   \
+  } while (0)
+
+// momentum_rhs_eq (src/transeq.f90:73-591) for the incompressible periodic
+// case, in operator precision T; writes the new right-hand side into h1,h2,h3.
+template <typename T, typename H>
+static int momentum_rhs(SolverImpl* s, const T* ux, const T* uy, const T* uz, H* hx, H* hy, H* hz, cudaStream_t st) {
+  Ctx* c = s->c;
+  const long long N = s->N;
+  const int dims[3] = {c->grid.nx, c->grid.ny, c->grid.nz};
+  T** w = reinterpret_cast<T**>(s->W);
+  T *ta = w[0], *tb = w[1], *tc = w[2], *td = w[3], *te = w[4], *tf = w[5];
+  T *tg1 = w[6], *th1 = w[7], *ti1 = w[8];
+  T *tg2 = w[9], *th2 = w[10], *ti2 = w[11];
+  const unsigned nb = pw_blocks(c, N);
+  const T xnu = (T)s->o.xnu;
+  // X stage
+  k_prod3<T><<<nb, 256, 0, st>>>(ta, tb, tc, ux, uy, uz, ux, N);
+  s->launches++;
+  RC(op<T>(s, 0, K_DER1, 1, td, ta, dims, st));
+  RC(op<T>(s, 0, K_DER1, 0, te, tb, dims, st));
+  RC(op<T>(s, 0, K_DER1, 0, tf, tc, dims, st));
+  RC(op<T>(s, 0, K_DER1, 0, ta, ux, dims, st));
+  RC(op<T>(s, 0, K_DER1, 1, tb, uy, dims, st));
+  RC(op<T>(s, 0, K_DER1, 1, tc, uz, dims, st));
+  k_addmul3<T><<<nb, 256, 0, st>>>(tg1, th1, ti1, td, te, tf, ta, tb, tc, ux, N);
+  s->launches++;
+  // Y stage
+  k_prod3<T><<<nb, 256, 0, st>>>(td, te, tf, ux, uy, uz, uy, N);
+  s->launches++;
+  RC(op<T>(s, 1, K_DER1, 0, tg2, td, dims, st));
+  RC(op<T>(s, 1, K_DER1, 1, th2, te, dims, st));
+  RC(op<T>(s, 1, K_DER1, 0, ti2, tf, dims, st));
+  RC(op<T>(s, 1, K_DER1, 1, td, ux, dims, st));
+  RC(op<T>(s, 1, K_DER1, 0, te, uy, dims, st));
+  RC(op<T>(s, 1, K_DER1, 1, tf, uz, dims, st));
+  k_addmul3<T><<<nb, 256, 0, st>>>(tg2, th2, ti2, tg2, th2, ti2, td, te, tf, uy, N);
+  s->launches++;
+  // Z stage: products, first derivatives, convective sum
+  k_prod3<T><<<nb, 256, 0, st>>>(td, te, tf, ux, uy, uz, uz, N);
+  s->launches++;
+  RC(op<T>(s, 2, K_DER1, 0, ta, td, dims, st));
+  RC(op<T>(s, 2, K_DER1, 0, tb, te, dims, st));
+  RC(op<T>(s, 2, K_DER1, 1, tc, tf, dims, st));
+  RC(op<T>(s, 2, K_DER1, 1, td, ux, dims, st));
+  RC(op<T>(s, 2, K_DER1, 1, te, uy, dims, st));
+  RC(op<T>(s, 2, K_DER1, 0, tf, uz, dims, st));
+  // ta3 = tg3 + uz*td3 (conv z), stored in ta/tb/tc
+  k_addmul3<T><<<nb, 256, 0, st>>>(ta, tb, tc, ta, tb, tc, td, te, tf, uz, N);
+  s->launches++;
+  // derzz into td/te/tf, then td3 = xnu*derzz - 0.5*conv_z
+  RC(op<T>(s, 2, K_DER2, 1, td, ux, dims, st));
+  RC(op<T>(s, 2, K_DER2, 1, te, uy, dims, st));
+  RC(op<T>(s, 2, K_DER2, 0, tf, uz, dims, st));
+  k_lin3<T><<<nb, 256, 0, st>>>(ta, tb, tc, td, te, tf, ta, tb, tc, xnu, T(-0.5), N);
+  s->launches++;
+  // back to Y: tg2 = td3 - 0.5*tg2
+  k_lin3<T><<<nb, 256, 0, st>>>(tg2, th2, ti2, ta, tb, tc, tg2, th2, ti2, T(1), T(-0.5), N);
+  s->launches++;
+  RC(op<T>(s, 1, K_DER2, 1, td, ux, dims, st));
+  RC(op<T>(s, 1, K_DER2, 0, te, uy, dims, st));
+  RC(op<T>(s, 1, K_DER2, 1, tf, uz, dims, st));
+  // ta2 = xnu*td2 + tg2
+  k_lin3<T><<<nb, 256, 0, st>>>(tg2, th2, ti2, td, te, tf, tg2, th2, ti2, xnu, T(1), N);
+  s->launches++;
+  // back to X: second derivatives and the final sum
+  RC(op<T>(s, 0, K_DER2, 0, td, ux, dims, st));
+  RC(op<T>(s, 0, K_DER2, 1, te, uy, dims, st));
+  RC(op<T>(s, 0, K_DER2, 1, tf, uz, dims, st));
+  k_final3<T, H><<<nb, 256, 0, st>>>(hx, hy, hz, tg2, th2, ti2, tg1, th1, ti1, td, te, tf, xnu, N);
+  s->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
+// divergence (nlock=1) of src/navier.f90:257-372: pp64 = div(u) on the
+// pressure mesh, computed in T, written in FP64 for the Poisson solve.
+template <typename T>
+static int divergence(SolverImpl* s, const T* ux, const T* uy, const T* uz, double* pp64, cudaStream_t st) {
+  Ctx* c = s->c;
+  const int nx = c->grid.nx, ny = c->grid.ny, nz = c->grid.nz;
+  const int nxm = c->ax[0].nm, nym = c->ax[1].nm;
+  T** p = reinterpret_cast<T**>(s->P);
+  T *pp1 = p[0], *pgy1 = p[1], *pgz1 = p[2], *upi2 = p[3], *duy = p[4], *pp3 = p[5], *po3 = p[6];
+  const int d1[3] = {nx, ny, nz};
+  RC(op<T>(s, 0, K_DVP, 0, pp1, ux, d1, st));
+  RC(op<T>(s, 0, K_IVP, 1, pgy1, uy, d1, st));
+  RC(op<T>(s, 0, K_IVP, 1, pgz1, uz, d1, st));
+  const int d2[3] = {nxm, ny, nz};
+  RC(op<T>(s, 1, K_IVP, 1, upi2, pp1, d2, st));
+  RC(op<T>(s, 1, K_DVP, 0, duy, pgy1, d2, st));
+  const long long n2 = (long long)nxm * c->ax[1].nm * nz;
+  k_add<T><<<pw_blocks(c, n2), 256, 0, st>>>(duy, duy, upi2, n2);
+  s->launches++;
+  RC(op<T>(s, 1, K_IVP, 1, upi2, pgz1, d2, st));
+  const int d3[3] = {nxm, nym, nz};
+  RC(op<T>(s, 2, K_IVP, 1, pp3, duy, d3, st));
+  RC(op<T>(s, 2, K_DVP, 0, po3, upi2, d3, st));
+  k_add_to64<T><<<pw_blocks(c, s->Np), 256, 0, st>>>(pp64, pp3, po3, s->Np);
+  s->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
+// gradp of src/navier.f90:386-499 (periodic: no wall-gradient storage).
+template <typename T>
+static int gradp(SolverImpl* s, const T* pp3, T* px, T* py, T* pz, cudaStream_t st) {
+  Ctx* c = s->c;
+  const int ny = c->grid.ny, nz = c->grid.nz;
+  const int nxm = c->ax[0].nm, nym = c->ax[1].nm, nzm = c->ax[2].nm;
+  T** p = reinterpret_cast<T**>(s->P);
+  T *ppi3 = p[0], *pgz3 = p[1], *ppi2 = p[2], *pgy2 = p[3], *pgzi2 = p[4];
+  const int d3[3] = {nxm, nym, nzm};
+  RC(op<T>(s, 2, K_IPV, 1, ppi3, pp3, d3, st));
+  RC(op<T>(s, 2, K_DPV, 1, pgz3, pp3, d3, st));
+  const int d2[3] = {nxm, nym, nz};
+  RC(op<T>(s, 1, K_IPV, 1, ppi2, ppi3, d2, st));
+  RC(op<T>(s, 1, K_DPV, 1, pgy2, ppi3, d2, st));
+  RC(op<T>(s, 1, K_IPV, 1, pgzi2, pgz3, d2, st));
+  const int d1[3] = {nxm, ny, nz};
+  RC(op<T>(s, 0, K_DPV, 1, px, ppi2, d1, st));
+  RC(op<T>(s, 0, K_IPV, 1, py, pgy2, d1, st));
+  RC(op<T>(s, 0, K_IPV, 1, pz, pgzi2, d1, st));
+  return X3D_OK;
+}
+
+template <typename T>
+static int substep(SolverImpl* s, int itr, cudaStream_t st) {
+  Ctx* c = s->c;
+  const long long N = s->N;
+  const unsigned nb = pw_blocks(c, N);
+  const bool mixed = std::is_same<T, float>::value;
+  const T* ux = mixed ? (const T*)s->ux32 : (const T*)s->ux;
+  const T* uy = mixed ? (const T*)s->uy32 : (const T*)s->uy;
+  const T* uz = mixed ? (const T*)s->uz32 : (const T*)s->uz;
+  T* hx = (T*)s->H[0][0];
+  T* hy = (T*)s->H[1][0];
+  T* hz = (T*)s->H[2][0];
+  RC((momentum_rhs<T, T>(s, ux, uy, uz, hx, hy, hz, st)));
+  // intt (src/time_integrators.f90:18-187); itime is the 1-based step index
+  const int it = s->itime + 1;
+  double* U[3] = {s->ux, s->uy, s->uz};
+  float* U32[3] = {s->ux32, s->uy32, s->uz32};
+  for (int q = 0; q < 3; ++q) {
+    const T* h1 = (const T*)s->H[q][0];
+    const T* h2 = (const T*)s->H[q][1];
+    const T* h3 = (const T*)s->H[q][2];
+    float* o32 = mixed ? U32[q] : nullptr;
+    const double dt = s->o.dt;
+    if (s->o.itimescheme == 3) {
+      if (it == 1) k_intt<T><<<nb, 256, 0, st>>>(U[q], o32, h1, nullptr, nullptr, dt, 0, 0, N);
+      else if (it == 2) k_intt<T><<<nb, 256, 0, st>>>(U[q], o32, h1, h2, nullptr, 1.5 * dt, -0.5 * dt, 0, N);
+      else k_intt<T><<<nb, 256, 0, st>>>(U[q], o32, h1, h2, h3, s->adt[0], s->bdt[0], s->cdt[0], N);
+    } else {
+      if (itr == 1) k_intt<T><<<nb, 256, 0, st>>>(U[q], o32, h1, nullptr, nullptr, s->gdt[0], 0, 0, N);
+      else k_intt<T><<<nb, 256, 0, st>>>(U[q], o32, h1, h2, nullptr, s->adt[itr - 1], s->bdt[itr - 1], 0, N);
+    }
+    s->launches++;
+  }
+  // history rotation: dvar(3)=dvar(2); dvar(2)=dvar(1)
+  for (int q = 0; q < 3; ++q) {
+    if (s->ntime == 3) {
+      void* t = s->H[q][2];
+      s->H[q][2] = s->H[q][1];
+      s->H[q][1] = s->H[q][0];
+      s->H[q][0] = t;
+    } else {
+      void* t = s->H[q][1];
+      s->H[q][1] = s->H[q][0];
+      s->H[q][0] = t;
+    }
+  }
+  RC(cuda_status(cudaGetLastError()));
+  // projection
+  const T* vx = mixed ? (const T*)s->ux32 : (const T*)s->ux;
+  const T* vy = mixed ? (const T*)s->uy32 : (const T*)s->uy;
+  const T* vz = mixed ? (const T*)s->uz32 : (const T*)s->uz;
+  RC(divergence<T>(s, vx, vy, vz, s->pp64, st));
+  RC(poisson_periodic(c, s->pp64, 0, st));
+  s->launches += 5;
+  const T* pin = (const T*)s->pp64;
+  T** w = reinterpret_cast<T**>(s->W);
+  if (mixed) {
+    k_to32<<<pw_blocks(c, s->Np), 256, 0, st>>>((float*)w[12], s->pp64, s->Np);
+    s->launches++;
+    pin = (const T*)w[12];
+  }
+  RC(gradp<T>(s, pin, w[0], w[1], w[2], st));
+  k_corvel<T><<<nb, 256, 0, st>>>(s->ux, s->uy, s->uz, mixed ? s->ux32 : nullptr, mixed ? s->uy32 : nullptr,
+                                  mixed ? s->uz32 : nullptr, w[0], w[1], w[2], N);
+  s->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
+static int solver_alloc(SolverImpl* s) {
+  Ctx* c = s->c;
+  const long long N = s->N;
+  const bool mixed = s->mixed();
+  const size_t es = mixed ? sizeof(float) : sizeof(double);
+  s->ux = s->alloc<double>(N);
+  s->uy = s->alloc<double>(N);
+  s->uz = s->alloc<double>(N);
+  if (!s->ux || !s->uy || !s->uz) return X3D_ERR_NOMEM;
+  if (mixed) {
+    s->ux32 = s->alloc<float>(N);
+    s->uy32 = s->alloc<float>(N);
+    s->uz32 = s->alloc<float>(N);
+    if (!s->ux32 || !s->uy32 || !s->uz32) return X3D_ERR_NOMEM;
+  }
+  for (int q = 0; q < 3; ++q)
+    for (int k = 0; k < s->ntime; ++k) {
+      s->H[q][k] = s->alloc<unsigned char>(N * (long long)es);
+      if (!s->H[q][k]) return X3D_ERR_NOMEM;
+      cudaMemset(s->H[q][k], 0, (size_t)N * es);
+    }
+  for (int k = 0; k < 13; ++k) {
+    s->W[k] = s->alloc<unsigned char>(N * (long long)es);
+    if (!s->W[k]) return X3D_ERR_NOMEM;
+  }
+  for (int k = 0; k < 7; ++k) {
+    s->P[k] = s->alloc<unsigned char>(N * (long long)es);
+    if (!s->P[k]) return X3D_ERR_NOMEM;
+  }
+  s->pp64 = s->alloc<double>(N);
+  s->part = s->alloc<double>(4LL * 4096);
+  if (!s->pp64 || !s->part) return X3D_ERR_NOMEM;
+  if (cudaMallocHost(&s->hpart, 4 * 4096 * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
+  (void)c;
+  return cuda_status(cudaGetLastError());
+}
+
+}  // namespace x3d
+
+using namespace x3d;
+
+extern "C" {
+
+int x3d_solver_create(x3d_ctx* ctx_, const x3d_solver_opts* o, x3d_solver** out) {
+  if (!ctx_ || !o || !out) return X3D_ERR_ARG;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx_);
+  if (!c->ax[0].periodic || !c->ax[1].periodic || !c->ax[2].periodic) return X3D_ERR_BC;
+  if (o->itimescheme != 3 && o->itimescheme != 5) return X3D_ERR_UNSUPPORTED;
+  if (o->precision != X3D_PREC_FP64 && o->precision != X3D_PREC_MIXED) return X3D_ERR_DTYPE;
+  x3d_solver* s = new x3d_solver();
+  SolverImpl* si = &s->impl;
+  si->c = c;
+  si->o = *o;
+  si->N = (long long)c->grid.nx * c->grid.ny * c->grid.nz;
+  si->Np = (long long)c->ax[0].nm * c->ax[1].nm * c->ax[2].nm;
+  const double dt = o->dt;
+  if (o->itimescheme == 3) {  // src/variables.f90:1366-1377
+    si->ntime = 3; si->nsub = 1;
+    si->adt[0] = (23.0 / 12.0) * dt; si->bdt[0] = -(16.0 / 12.0) * dt; si->cdt[0] = (5.0 / 12.0) * dt;
+    si->gdt[0] = si->adt[0] + si->bdt[0] + si->cdt[0];
+  } else {  // RK3, src/variables.f90:1389-1400
+    si->ntime = 2; si->nsub = 3;
+    si->adt[0] = (8.0 / 15.0) * dt; si->bdt[0] = 0.0; si->gdt[0] = si->adt[0];
+    si->adt[1] = (5.0 / 12.0) * dt; si->bdt[1] = (-17.0 / 60.0) * dt; si->gdt[1] = si->adt[1] + si->bdt[1];
+    si->adt[2] = (3.0 / 4.0) * dt; si->bdt[2] = (-5.0 / 12.0) * dt; si->gdt[2] = si->adt[2] + si->bdt[2];
+  }
+  int rc = solver_alloc(si);
+  if (rc != X3D_OK) {
+    delete s;
+    return rc;
+  }
+  *out = s;
+  return X3D_OK;
+}
+
+int x3d_solver_destroy(x3d_solver* s) {
+  delete s;
+  return X3D_OK;
+}
+
+static int sync_copies(SolverImpl* s) {
+  if (!s->mixed()) return X3D_OK;
+  Ctx* c = s->c;
+  const unsigned nb = pw_blocks(c, s->N);
+  k_to32<<<nb, 256>>>(s->ux32, s->ux, s->N);
+  k_to32<<<nb, 256>>>(s->uy32, s->uy, s->N);
+  k_to32<<<nb, 256>>>(s->uz32, s->uz, s->N);
+  return cuda_status(cudaDeviceSynchronize());
+}
+
+int x3d_solver_set_velocity(x3d_solver* s, const double* ux, const double* uy, const double* uz, int on_device) {
+  if (!s || !ux || !uy || !uz) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  const size_t b = (size_t)si->N * sizeof(double);
+  const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (cudaMemcpy(si->ux, ux, b, k) != cudaSuccess || cudaMemcpy(si->uy, uy, b, k) != cudaSuccess ||
+      cudaMemcpy(si->uz, uz, b, k) != cudaSuccess)
+    return X3D_ERR_CUDA;
+  si->itime = 0;
+  return sync_copies(si);
+}
+
+int x3d_solver_get_velocity(x3d_solver* s, double* ux, double* uy, double* uz, int on_device) {
+  if (!s || !ux || !uy || !uz) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  const size_t b = (size_t)si->N * sizeof(double);
+  const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (cudaMemcpy(ux, si->ux, b, k) != cudaSuccess || cudaMemcpy(uy, si->uy, b, k) != cudaSuccess ||
+      cudaMemcpy(uz, si->uz, b, k) != cudaSuccess)
+    return X3D_ERR_CUDA;
+  return X3D_OK;
+}
+
+int x3d_solver_init_tgv(x3d_solver* s) {
+  if (!s) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  Ctx* c = si->c;
+  k_tgv_init<<<pw_blocks(c, si->N), 256>>>(si->ux, si->uy, si->uz, c->grid.nx, c->grid.ny, c->grid.nz, c->ax[0].d,
+                                           c->ax[1].d, c->ax[2].d);
+  si->itime = 0;
+  int rc = cuda_status(cudaGetLastError());
+  if (rc != X3D_OK) return rc;
+  return sync_copies(si);
+}
+
+int x3d_solver_step(x3d_solver* s, int nsteps, void* stream) {
+  if (!s || nsteps < 0) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  cudaStream_t st = (cudaStream_t)stream;
+  for (int n = 0; n < nsteps; ++n) {
+    for (int itr = 1; itr <= si->nsub; ++itr) {
+      const int rc = si->mixed() ? substep<float>(si, itr, st) : substep<double>(si, itr, st);
+      if (rc != X3D_OK) return rc;
+    }
+    si->itime++;
+  }
+  return X3D_OK;
+}
+
+int x3d_solver_launches_per_step(x3d_solver* s) {
+  if (!s) return X3D_ERR_ARG;
+  return s->impl.launches / (s->impl.itime > 0 ? s->impl.itime : 1);
+}
+
+int x3d_solver_tgv_stats(x3d_solver* s, double* out, void* stream) {
+  if (!s || !out) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  Ctx* c = si->c;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int dims[3] = {c->grid.nx, c->grid.ny, c->grid.nz};
+  // 9 first + 9 second derivatives in FP64 (postprocess_tgv), in FP64 buffers
+  std::vector<double*> g(9), l(9);
+  double* buf = nullptr;
+  if (cudaMalloc(&buf, (size_t)18 * si->N * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
+  for (int q = 0; q < 9; ++q) { g[q] = buf + (size_t)q * si->N; l[q] = buf + (size_t)(9 + q) * si->N; }
+  const double* u[3] = {si->ux, si->uy, si->uz};
+  // parity as in src/Case-TGV.f90:246-264: d(u)/dx odd(0), d(v)/dx even(1), ...
+  const int par1[3][3] = {{0, 1, 1}, {1, 0, 1}, {1, 1, 0}};  // [axis][component]
+  int rc = X3D_OK;
+  for (int a = 0; a < 3 && rc == X3D_OK; ++a)
+    for (int q = 0; q < 3 && rc == X3D_OK; ++q) {
+      OpPlan* p1 = nullptr;
+      OpPlan* p2 = nullptr;
+      const int np = par1[a][q];
+      rc = get_plan(c, a, K_DER1, np, default_coefset(K_DER1, np), &p1);
+      if (rc == X3D_OK) rc = get_plan(c, a, K_DER2, np, default_coefset(K_DER2, np), &p2);
+      if (rc == X3D_OK) rc = launch_line_op<double>(c, p1, g[a * 3 + q], u[q], dims, nullptr, st);
+      if (rc == X3D_OK) rc = launch_line_op<double>(c, p2, l[a * 3 + q], u[q], dims, nullptr, st);
+    }
+  if (rc == X3D_OK) {
+    double** dg = nullptr;
+    cudaMalloc(&dg, 18 * sizeof(double*));
+    std::vector<double*> all(g);
+    all.insert(all.end(), l.begin(), l.end());
+    cudaMemcpyAsync(dg, all.data(), 18 * sizeof(double*), cudaMemcpyHostToDevice, st);
+    const unsigned nb = std::min<unsigned>(4096, pw_blocks(c, si->N));
+    k_stats<<<nb, 256, 0, st>>>(si->ux, si->uy, si->uz, dg, dg + 9, si->o.xnu, si->N, si->part);
+    cudaMemcpyAsync(si->hpart, si->part, (size_t)nb * 4 * sizeof(double), cudaMemcpyDeviceToHost, st);
+    rc = cuda_status(cudaStreamSynchronize(st));
+    double acc[4] = {0, 0, 0, 0};
+    for (unsigned b = 0; b < nb; ++b)
+      for (int q = 0; q < 4; ++q) acc[q] += si->hpart[(size_t)b * 4 + q];
+    const double nc = (double)si->N;
+    out[0] = acc[0] / nc;
+    out[1] = acc[1] / nc;
+    out[2] = acc[3] / nc;
+    out[3] = acc[2] / nc;
+    cudaFree(dg);
+  }
+  cudaFree(buf);
+  return rc;
+}
+
+int x3d_solver_divmax(x3d_solver* s, double* out, void* stream) {
+  if (!s || !out) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  Ctx* c = si->c;
+  cudaStream_t st = (cudaStream_t)stream;
+  // always evaluated in FP64 on the FP64 state
+  double* tmp = nullptr;
+  double* P[7];
+  if (cudaMalloc(&tmp, (size_t)8 * si->N * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
+  for (int k = 0; k < 7; ++k) P[k] = tmp + (size_t)k * si->N;
+  void* saveP[8];
+  std::memcpy(saveP, si->P, sizeof(saveP));
+  for (int k = 0; k < 7; ++k) si->P[k] = P[k];
+  double* dv = tmp + (size_t)7 * si->N;
+  int rc = divergence<double>(si, si->ux, si->uy, si->uz, dv, st);
+  std::memcpy(si->P, saveP, sizeof(saveP));
+  if (rc == X3D_OK) {
+    const unsigned nb = std::min<unsigned>(4096, pw_blocks(c, si->Np));
+    k_absmax<<<nb, 256, 0, st>>>(dv, si->Np, si->part);
+    cudaMemcpyAsync(si->hpart, si->part, nb * sizeof(double), cudaMemcpyDeviceToHost, st);
+    rc = cuda_status(cudaStreamSynchronize(st));
+    double m = 0;
+    for (unsigned b = 0; b < nb; ++b) m = std::max(m, si->hpart[b]);
+    *out = m;
+  }
+  cudaFree(tmp);
+  return rc;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Stand-alone projection pieces (C ABI), FP64, on context scratch.
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int x3d_divergence(x3d_ctx* h, double* pp3, const double* ux, const double* uy, const double* uz, void* stream) {
+  if (!h || !pp3 || !ux || !uy || !uz) return X3D_ERR_ARG;
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  SolverImpl s;
+  s.c = c;
+  s.N = (long long)c->grid.nx * c->grid.ny * c->grid.nz;
+  s.Np = (long long)c->ax[0].nm * c->ax[1].nm * c->ax[2].nm;
+  void* ws = nullptr;
+  int rc = ctx_workspace(c, (size_t)7 * s.N * sizeof(double), &ws);
+  if (rc != X3D_OK) return rc;
+  for (int k = 0; k < 7; ++k) s.P[k] = (double*)ws + (size_t)k * s.N;
+  return divergence<double>(&s, ux, uy, uz, pp3, (cudaStream_t)stream);
+}
+
+int x3d_gradp(x3d_ctx* h, double* px, double* py, double* pz, const double* pp3, void* stream) {
+  if (!h || !px || !py || !pz || !pp3) return X3D_ERR_ARG;
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  SolverImpl s;
+  s.c = c;
+  s.N = (long long)c->grid.nx * c->grid.ny * c->grid.nz;
+  void* ws = nullptr;
+  int rc = ctx_workspace(c, (size_t)5 * s.N * sizeof(double), &ws);
+  if (rc != X3D_OK) return rc;
+  for (int k = 0; k < 5; ++k) s.P[k] = (double*)ws + (size_t)k * s.N;
+  return gradp<double>(&s, pp3, px, py, pz, (cudaStream_t)stream);
+}
+
+int x3d_cor_vel(x3d_ctx* h, double* ux, double* uy, double* uz, const double* px, const double* py,
+                const double* pz, void* stream) {
+  if (!h || !ux || !uy || !uz || !px || !py || !pz) return X3D_ERR_ARG;
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  const long long N = (long long)c->grid.nx * c->grid.ny * c->grid.nz;
+  k_corvel<double><<<pw_blocks(c, N), 256, 0, (cudaStream_t)stream>>>(ux, uy, uz, nullptr, nullptr, nullptr, px, py,
+                                                                      pz, N);
+  return cuda_status(cudaGetLastError());
+}
+
+}  // extern "C"

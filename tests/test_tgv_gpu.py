@@ -1,0 +1,73 @@
+"""Taylor-Green vortex on the GPU solver vs the CPU oracle.
+
+Configuration: 64^3 triply periodic on [0,2pi]^3, Re=1600, AB3 (Euler and AB2
+start-up, src/time_integrators.f90:86-100), dt=0.005, 200 steps, statistics of
+postprocess_tgv (src/Case-TGV.f90:189-477) every 10 steps.  FP64 must match the
+oracle within 1e-10 (relative); the mixed-precision solver must keep the
+kinetic energy within 1e-6 of the FP64 run.
+"""
+import numpy as np
+import pytest
+
+from conftest import relerr
+
+pytestmark = pytest.mark.gpu
+L = 2 * np.pi
+
+
+def tgv_ic(n):
+    x = np.arange(n) * (L / n)
+    X, Y, Z = x[None, None, :], x[None, :, None], x[:, None, None]
+    ux = np.sin(X) * np.cos(Y) * np.cos(Z)
+    uy = -np.cos(X) * np.sin(Y) * np.cos(Z)
+    return ux, uy, np.zeros_like(ux)
+
+
+def run_gpu(gpu_lib, n, nsteps, dt, itimescheme, precision, every=10):
+    ctx = gpu_lib.Context(n, n, n, L, L, L)
+    s = gpu_lib.Solver(ctx, dt, 1 / 1600.0, itimescheme=itimescheme, precision=precision)
+    s.set_velocity(*tgv_ic(n))
+    rows = []
+    for it in range(1, nsteps + 1):
+        s.step(1)
+        if it % every == 0:
+            rows.append([(it - 1) * dt, *s.tgv_stats()])
+    return np.array(rows), s, ctx
+
+
+@pytest.fixture(scope="module")
+def oracle_tgv64(oracle_mod):
+    o = oracle_mod.Oracle(64, 64, 64, L, L, L)
+    ux, uy, uz = tgv_ic(64)
+    a, b, c, rows, dmax = o.run(ux, uy, uz, 200, 0.005, 1 / 1600.0, 3, 10)
+    return rows, (a, b, c), dmax
+
+
+def test_tgv64_ab3_fp64_matches_oracle(gpu_lib, oracle_tgv64):
+    rows_o, u_o, dmax_o = oracle_tgv64
+    rows, s, ctx = run_gpu(gpu_lib, 64, 200, 0.005, 3, gpu_lib.PREC_FP64)
+    assert rows.shape == rows_o.shape == (20, 5)
+    for col, name in ((1, "E_k"), (2, "eps"), (3, "eps2"), (4, "enstrophy")):
+        err = np.max(np.abs(rows[:, col] - rows_o[:, col]) / np.abs(rows_o[:, col]))
+        assert err < 1e-10, (name, err)
+    u = s.get_velocity()
+    for a, b in zip(u, u_o):
+        assert relerr(a, b) < 1e-10
+    assert s.divmax() < 1e-12
+
+
+def test_tgv64_mixed_precision_energy(gpu_lib, oracle_tgv64):
+    rows_o, _, _ = oracle_tgv64
+    rows, s, ctx = run_gpu(gpu_lib, 64, 200, 0.005, 3, gpu_lib.PREC_MIXED)
+    ke_err = np.max(np.abs(rows[:, 1] - rows_o[:, 1]))
+    assert ke_err < 1e-6, ke_err
+    assert s.divmax() < 1e-5
+
+
+def test_tgv_rk3_matches_oracle(oracle_mod, gpu_lib):
+    n = 32
+    o = oracle_mod.Oracle(n, n, n, L, L, L)
+    ux, uy, uz = tgv_ic(n)
+    _, _, _, rows_o, _ = o.run(ux, uy, uz, 20, 0.01, 1 / 1600.0, 5, 10)
+    rows, s, ctx = run_gpu(gpu_lib, n, 20, 0.01, 5, gpu_lib.PREC_FP64)
+    assert np.max(np.abs(rows[:, 1:] - rows_o[:, 1:]) / np.abs(rows_o[:, 1:])) < 1e-10
