@@ -76,6 +76,9 @@ typedef struct {
 int x3d_ctx_create(const x3d_grid* grid, const x3d_numopts* opts, x3d_ctx** out);
 int x3d_ctx_destroy(x3d_ctx* ctx);
 const char* x3d_strerror(int status);
+/* Text of the CUDA runtime error behind the calling thread's most recent
+ * X3D_ERR_CUDA status (diagnostics; no counterpart in the reference). */
+const char* x3d_last_cuda_error(void);
 
 /* Host copy of a coefficient vector, so a Fortran or C caller can pass the
  * same arrays the reference passes.  axis 0..2; `which` uses the numbering of
@@ -180,6 +183,15 @@ int x3d_interzpv(x3d_ctx* ctx, double* tz, const double* uz, double* rz, double*
  * 0 = plain set, 1 = "p" set. */
 int x3d_apply(x3d_ctx* ctx, int axis, int op, int npaire, int coefset, int dtype, void* t, const void* u,
               const int* dims_in, void* stream);
+
+/* Host-side description of the plan x3d_apply uses for (axis, op, npaire,
+ * coefset): the line kernel's interior coefficients, Thomas factors,
+ * chunked-solve fix-up factors, Sherman-Morrison vector and boundary-row
+ * table (layout documented in incompact3d_gb300/csrc/x3d_internal.h).  No
+ * device work; returns the output line length or a negative status.  Has no
+ * counterpart in the reference (diagnostics). */
+int x3d_plan_info(x3d_ctx* ctx, int axis, int op, int npaire, int coefset, double* scalars, double* vecs,
+                  double* brows);
 
 /* --- single-precision builds of the derivative / filter routines ---------- */
 int x3d_derx_f32(x3d_ctx* ctx, float* tx, const float* ux, int nx, int ny, int nz, int npaire, void* stream);

@@ -33,7 +33,10 @@ COEF = {n: i for i, n in enumerate(COEF_NAMES)}
 class X3DError(RuntimeError):
     def __init__(self, status, what=""):
         self.status = status
-        super().__init__("%s failed: %s (%d)" % (what, ERRORS.get(status, "?"), status))
+        msg = "%s failed: %s (%d)" % (what, ERRORS.get(status, "?"), status)
+        if status == -5 and _lib is not None:
+            msg += ": " + _lib.x3d_last_cuda_error().decode()
+        super().__init__(msg)
 
 
 class Grid(ctypes.Structure):
@@ -78,10 +81,13 @@ def load():
         P, I, D, LL = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
         lib.x3d_strerror.restype = ctypes.c_char_p
         lib.x3d_strerror.argtypes = [I]
+        lib.x3d_last_cuda_error.restype = ctypes.c_char_p
+        lib.x3d_last_cuda_error.argtypes = []
         lib.x3d_ctx_create.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(NumOpts), ctypes.POINTER(P)]
         lib.x3d_ctx_destroy.argtypes = [P]
         lib.x3d_get_coeffs.argtypes = [P, I, I, P, I]
         lib.x3d_apply.argtypes = [P, I, I, I, I, I, P, P, P, P]
+        lib.x3d_plan_info.argtypes = [P, I, I, I, I, P, P, P]
         colloc = [P, P, P, P, P, P, P, P, I, I, I, I, D, P]
         for n in ("derx", "derz", "derxx", "deryy", "derzz", "filx", "fily", "filz"):
             getattr(lib, "x3d_" + n).argtypes = colloc

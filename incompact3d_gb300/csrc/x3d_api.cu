@@ -22,6 +22,9 @@ Ctx::~Ctx() {
   if (fft_work) cudaFree(fft_work);
 }
 
+static thread_local cudaError_t g_last_cuda = cudaSuccess;
+void note_cuda_error(cudaError_t e) { g_last_cuda = e; }
+
 int ctx_workspace(Ctx* c, size_t bytes, void** out) {
   if (!c->ws) c->ws.reset(new Workspace());
   Workspace* w = c->ws.get();
@@ -48,11 +51,7 @@ int get_plan(Ctx* c, int axis, int kind, int npaire, int coefset, OpPlan** out) 
   int rc = build_plan(c->ax[axis], axis, kind, npaire, coefset, *p);
   if (rc != X3D_OK) return rc;
   rc = finalize_plan(p.get());
-  if (rc != X3D_OK) {
-    if (p->dev64) cudaFree(p->dev64);
-    if (p->dev32) cudaFree(p->dev32);
-    return rc;
-  }
+  if (rc != X3D_OK) return rc;
   *out = p.get();
   c->plans[key] = std::move(p);
   return X3D_OK;
@@ -161,6 +160,10 @@ int stag(x3d_ctx* h, int axis, int kind, double* t, const double* u, const doubl
 
 extern "C" {
 
+const char* x3d_last_cuda_error(void) {
+  return g_last_cuda == cudaSuccess ? "no CUDA error recorded" : cudaGetErrorString(g_last_cuda);
+}
+
 const char* x3d_strerror(int s) {
   switch (s) {
     case X3D_OK: return "ok";
@@ -224,6 +227,14 @@ int x3d_apply(x3d_ctx* h, int axis, int op, int npaire, int coefset, int dtype, 
   if (dtype == 0) return run_op<double>(h, axis, op, npaire, coefset, (double*)t, (const double*)u, dims_in, stream);
   if (dtype == 1) return run_op<float>(h, axis, op, npaire, coefset, (float*)t, (const float*)u, dims_in, stream);
   return X3D_ERR_DTYPE;
+}
+
+int x3d_plan_info(x3d_ctx* h, int axis, int op, int npaire, int coefset, double* scalars, double* vecs,
+                  double* brows) {
+  if (!h) return X3D_ERR_ARG;
+  if (coefset == -1) coefset = default_coefset(op, npaire);
+  if (coefset != 0 && coefset != 1 || (npaire != 0 && npaire != 1)) return X3D_ERR_ARG;
+  return plan_info(C(h), axis, op, npaire, coefset, scalars, vecs, brows);
 }
 
 // ---- derivatives and filters -----------------------------------------------

@@ -124,9 +124,19 @@ int get_plan(Ctx* c, int axis, int kind, int npaire, int coefset, OpPlan** out);
 template <typename T>
 int launch_line_op(Ctx* c, OpPlan* p, T* out, const T* in, const int* dims_in, const T* pp, cudaStream_t st);
 
+// Host copy of a plan: sc[16] scalars, vecs[6*nout] = s,f,w,pf,qb,rsm,
+// brows[kMaxBRows*(2+kMaxTerms*(2+2*kMaxEnt))].  Returns nout or an error.
+int plan_info(Ctx* c, int axis, int kind, int npaire, int coefset, double* sc, double* vecs, double* brows);
+
 // Poisson (periodic, all three directions).  precision 0: FP64 FFT, 1: FP32 FFT.
 int poisson_periodic(Ctx* c, double* rhs, int precision, cudaStream_t st);
 
-inline int cuda_status(cudaError_t e) { return e == cudaSuccess ? X3D_OK : X3D_ERR_CUDA; }
+// Records the CUDA error behind an X3D_ERR_CUDA (see x3d_last_cuda_error).
+void note_cuda_error(cudaError_t e);
+inline int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return X3D_OK;
+  note_cuda_error(e);
+  return X3D_ERR_CUDA;
+}
 
 }  // namespace x3d

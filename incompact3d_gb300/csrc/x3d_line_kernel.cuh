@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(LANES* CHUNKS) line_kernel(const __grid_consta
     if (ch == 0) ends[lane] = v[0];
 #pragma unroll
     for (int k = 0; k < LMAX; ++k)
-      if (r0 + k == nout - 1) ends[LANES + lane] = v[k];
+      if (r0 + k < r1 && r0 + k == nout - 1) ends[LANES + lane] = v[k];
     __syncthreads();
     const T sx = (ends[lane] - p.alpha * ends[LANES + lane]) / p.den;
 #pragma unroll
@@ -271,11 +271,11 @@ size_t line_smem(int nin, int nout) {
 template <typename T, int KIND, bool XL, int LMAX>
 int launch_k(const LineArgs<T>& a, dim3 grid, size_t smem, cudaStream_t st) {
   auto kern = line_kernel<T, KIND, XL, LMAX>;
-  static bool configured = false;  // attribute is per-function, per-device; cheap to repeat
-  if (!configured || smem > 48 * 1024) {
+  static size_t configured = 0;  // largest dynamic smem opted in so far (per instantiation)
+  if (smem > configured) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return X3D_ERR_CUDA;
-    configured = true;
+    if (e != cudaSuccess) return cuda_status(e);
+    configured = smem;
   }
   kern<<<grid, dim3(LANES, CHUNKS), smem, st>>>(a);
   return cuda_status(cudaGetLastError());

@@ -32,7 +32,7 @@ const float* plan_dev<float>(const OpPlan* p) { return p->dev32; }
 
 }  // namespace
 
-// Chunk length and fix-up factors for a plan (host), plus device upload.
+// Chunk length and fix-up factors for a plan (host only).
 int finalize_plan(OpPlan* p) {
   const int n = p->nout;
   const int L = (n + CHUNKS - 1) / CHUNKS;
@@ -53,6 +53,13 @@ int finalize_plan(OpPlan* p) {
       p->qb[r] = acc;
     }
   }
+  return X3D_OK;
+}
+
+// Device copies of a plan's vectors, made on first launch.
+static int upload_plan(OpPlan* p) {
+  if (p->dev64) return X3D_OK;
+  const int n = p->nout;
   std::vector<double> h64(6 * (size_t)n);
   std::vector<float> h32(6 * (size_t)n);
   const dvec* parts[6] = {&p->s, &p->f, &p->w, &p->pf, &p->qb, &p->rsm};
@@ -61,12 +68,22 @@ int finalize_plan(OpPlan* p) {
       h64[(size_t)q * n + r] = (*parts[q])[r];
       h32[(size_t)q * n + r] = (float)(*parts[q])[r];
     }
-  if (cudaMalloc(&p->dev64, h64.size() * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
-  if (cudaMalloc(&p->dev32, h32.size() * sizeof(float)) != cudaSuccess) return X3D_ERR_NOMEM;
-  if (cudaMemcpy(p->dev64, h64.data(), h64.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
-    return X3D_ERR_CUDA;
-  if (cudaMemcpy(p->dev32, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
-    return X3D_ERR_CUDA;
+  double* d64 = nullptr;
+  float* d32 = nullptr;
+  if (cudaMalloc(&d64, h64.size() * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
+  if (cudaMalloc(&d32, h32.size() * sizeof(float)) != cudaSuccess) {
+    cudaFree(d64);
+    return X3D_ERR_NOMEM;
+  }
+  cudaError_t e = cudaMemcpy(d64, h64.data(), h64.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d32, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(d64);
+    cudaFree(d32);
+    return cuda_status(e);
+  }
+  p->dev64 = d64;
+  p->dev32 = d32;
   return X3D_OK;
 }
 
@@ -75,6 +92,8 @@ int launch_line_op(Ctx* c, OpPlan* p, T* out, const T* in, const int* dims_in, c
   (void)c;
   if (!out || !in) return X3D_ERR_ARG;
   if (dims_in[p->axis] != p->nin) return X3D_ERR_SHAPE;
+  const int up = upload_plan(p);
+  if (up != X3D_OK) return up;
   LineArgs<T> a;
   std::memset(&a, 0, sizeof(a));
   a.in = in;
@@ -132,6 +151,40 @@ int launch_line_op(Ctx* c, OpPlan* p, T* out, const T* in, const int* dims_in, c
   const size_t smem = line_smem<T>(p->nin, p->nout);
   if (smem > 227 * 1024) return X3D_ERR_UNSUPPORTED;
   return dispatch<T>(a, p->kind, xl, lmax, grid, smem, st);
+}
+
+// Host copy of a plan (diagnostics / CPU emulation of the kernel).
+int plan_info(Ctx* c, int axis, int kind, int npaire, int coefset, double* sc, double* vecs, double* brows) {
+  OpPlan* p = nullptr;
+  const int rc = get_plan(c, axis, kind, npaire, coefset, &p);
+  if (rc != X3D_OK) return rc;
+  const int n = p->nout;
+  int nt = 4;
+  if (p->kind == K_DER2 && p->cc == 0.0 && p->cd == 0.0) nt = 2;
+  if ((p->kind == K_IVP || p->kind == K_IPV) && p->cd == 0.0) nt = 3;
+  const double v[16] = {(double)p->nin, (double)n, (double)p->L, p->periodic ? 1.0 : 0.0, p->ca, p->cb, p->cc,
+                        p->cd, p->alpha, p->den, (double)p->nbrows, (double)nt, (double)CHUNKS, 0, 0, 0};
+  if (sc) std::memcpy(sc, v, sizeof(v));
+  const dvec* parts[6] = {&p->s, &p->f, &p->w, &p->pf, &p->qb, &p->rsm};
+  if (vecs)
+    for (int q = 0; q < 6; ++q) std::memcpy(vecs + (size_t)q * n, parts[q]->data(), n * sizeof(double));
+  if (brows)
+    for (int q = 0; q < p->nbrows; ++q) {
+      const BRow& b = p->brows[q];
+      double* o = brows + q * (2 + kMaxTerms * (2 + 2 * kMaxEnt));
+      o[0] = b.row;
+      o[1] = b.nterms;
+      for (int t = 0; t < kMaxTerms; ++t) {
+        double* ot = o + 2 + t * (2 + 2 * kMaxEnt);
+        ot[0] = b.coef[t];
+        ot[1] = b.nent[t];
+        for (int e = 0; e < kMaxEnt; ++e) {
+          ot[2 + 2 * e] = b.idx[t][e];
+          ot[3 + 2 * e] = b.mult[t][e];
+        }
+      }
+    }
+  return n;
 }
 
 template int launch_line_op<double>(Ctx*, OpPlan*, double*, const double*, const int*, const double*, cudaStream_t);

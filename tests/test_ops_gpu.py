@@ -3,8 +3,9 @@
 Each operator (first/second derivative, filter, the four staggered operators)
 along x, y and z, for every boundary-condition pair and parity the reference
 implements (src/derive.f90, src/filters.f90), in FP64 and FP32, called through
-the C ABI.  Tolerances: FP64 1e-12 relative to the field's max (the parity
-bound of the task); FP32 2e-5.
+the C ABI.  Tolerances, relative to the field's max: FP64 1e-12 (the parity
+bound); FP32 1e-4 (binary32 round-off amplified by the one-sided Dirichlet
+closures of the second derivative, whose coefficients are O(10/dx^2)).
 """
 import numpy as np
 import pytest
@@ -15,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 OPS = ["der1", "der2", "fil", "dvp", "ivp", "dpv", "ipv"]
 BCS = [(0, 0), (1, 1), (2, 2), (1, 2), (2, 1)]
-TOL = {"float64": 1e-12, "float32": 2e-5}
+TOL = {"float64": 1e-12, "float32": 1e-4}
 
 
 def _cases():
