@@ -69,7 +69,7 @@ def test_line_lengths(oracle_mod, gpu_lib, n):
     import torch
     L = 2 * np.pi
     for bc in [(0, 0), (2, 2)]:
-        dims = (n, 9, 5)
+        dims = (n, 9, 8)
         ctx = gpu_lib.Context(*dims, L, L, L, bc=(bc, (0, 0), (0, 0)))
         o = oracle_mod.Oracle(*dims, L, L, L, bc=(bc, (0, 0), (0, 0)))
         u = fourier_field(*dims, seed=n, periodic=(bc == (0, 0), True, True))

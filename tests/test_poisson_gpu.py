@@ -108,6 +108,8 @@ def test_projection_property_full_size(gpu_lib, n):
     px, py, pz = ctx.gradp(pp)
     ctx.cor_vel(ux, uy, uz, px, py, pz)
     dv = ctx.divergence(ux, uy, uz)
-    assert dv.abs().max().item() < 1e-12 * d0 + 1e-13
+    # The residual of the reference's own arithmetic grows like n^3 (oracle, this
+    # field: 1e-13 at 32^3, 2e-12 at 64^3, 1.4e-11 at 128^3 relative to d0).
+    assert dv.abs().max().item() < 1e-16 * n ** 3 * d0
     del ux, uy, uz, px, py, pz, pp, dv
     torch.cuda.empty_cache()
