@@ -202,6 +202,13 @@ def run_ours(args):
     if len(solvers) == 2:
         for prec, s in solvers.items():
             ke[prec] = float(s.tgv_stats()[0])
+    if args.no_e2e:
+        if rank == 0:
+            main = res.get("mixed") or res[list(res)[0]]
+            print(json.dumps({"metric": METRIC, "value": round(N * args.steps * ws / main["secs"] / 1e6, 3),
+                              "unit": UNIT, "steps": args.steps, "warmup": args.warmup,
+                              "ms_per_step": round(1e3 * main["secs"] / args.steps, 3), "partial": "no e2e"}))
+        return
     # e2e through the public API with host buffers: H2D velocity (pinned) ->
     # one step -> D2H velocity, every step, on the mixed solver
     e2e = None
@@ -287,6 +294,8 @@ def main():
     ap.add_argument("--cpu-n", type=int, default=64)
     ap.add_argument("--ref-n", type=int, default=128)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true",
+                    help="profiling runs: time the step loop only (no e2e, kernel or CPU legs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -55,6 +55,11 @@ struct LineArgs {
   BRowD<T> brows[kMaxBRows];
 };
 
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+
 template <int KIND>
 struct Ext;
 template <> struct Ext<K_DER1> { static constexpr int lo = -2, hi = 2; };
@@ -106,14 +111,17 @@ __device__ __forceinline__ T rhs_row(const LineArgs<T>& p, const T* tile, int la
     };
     return interior<T, KIND>(U, r, p);
   }
+  // Boundary rows: unfused round-to-nearest operations in the reference's
+  // order.  The one-sided closures sum terms of size ~u/dx^2 that cancel, so
+  // fusing would change the result well above round-off of the output.
   for (int q = 0; q < p.nbrows; ++q) {
     const BRowD<T>& b = p.brows[q];
     if (b.row != r) continue;
     T acc = T(0);
     for (int t = 0; t < b.nterms; ++t) {
-      T v = T(b.mult[t][0]) * tile[b.idx[t][0] * LD + lane];
-      for (int e = 1; e < b.nent[t]; ++e) v = v + T(b.mult[t][e]) * tile[b.idx[t][e] * LD + lane];
-      acc = (t == 0) ? b.coef[t] * v : acc + b.coef[t] * v;
+      T v = T(b.mult[t][0]) * tile[b.idx[t][0] * LD + lane];  // mult = +-1, +-2: exact
+      for (int e = 1; e < b.nent[t]; ++e) v = add_rn(v, T(b.mult[t][e]) * tile[b.idx[t][e] * LD + lane]);
+      acc = (t == 0) ? mul_rn(b.coef[t], v) : add_rn(acc, mul_rn(b.coef[t], v));
     }
     return acc;
   }
