@@ -42,7 +42,8 @@ enum {
   X3D_ERR_COEF = -6,        /* coefficient vectors match no context set       */
   X3D_ERR_UNSUPPORTED = -7, /* option outside the implemented scope           */
   X3D_ERR_NOMEM = -8,       /* device allocation failed                       */
-  X3D_ERR_STATE = -9        /* solver not initialised / numerical blow-up     */
+  X3D_ERR_STATE = -9,       /* solver not initialised / numerical blow-up     */
+  X3D_ERR_SCRATCH = -10     /* too large for the allocation-free entry point  */
 };
 
 typedef struct x3d_ctx x3d_ctx;
@@ -210,6 +211,24 @@ int x3d_filz_f32(x3d_ctx* ctx, float* tz, const float* uz, int nx, int ny, int n
  * overwritten by the solution.  precision: 0 = FP64 FFT, 1 = FP32 FFT. */
 int x3d_poisson(x3d_ctx* ctx, double* rhs, void* stream);
 int x3d_poisson_ex(x3d_ctx* ctx, double* rhs, int precision, void* stream);
+
+/* Allocation-free form of x3d_poisson (FP64 FFT), for callers that cannot
+ * allocate device memory when they solve: codes whose device memory is
+ * reserved up front in their own pool and that treat any later allocation as
+ * an error.  x3d_poisson allocates its spectrum and tables in the context on
+ * first use; this entry point instead uses one fixed array of
+ * X3D_NOALLOC_SCRATCH_BYTES in the library's device image (held by every GPU
+ * that loads the library until the process exits) and calls no allocating
+ * routine.  The spectrum needs (nx/2+1)*ny*nz*16 bytes plus small tables;
+ * larger grids return X3D_ERR_SCRATCH (e.g. 128^3 fits, 256^3 does not).  The
+ * array is shared by every call from any context or stream and keeps the last
+ * call's contents (each call rewrites everything it reads), so calls that
+ * overlap on the GPU race.  The first call on each device looks up the
+ * array's device address with that device current; make that first call
+ * before any stream capture.  Same argument meaning and result as
+ * x3d_poisson.  No counterpart in the reference. */
+#define X3D_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+int x3d_poisson_noalloc(x3d_ctx* ctx, double* rhs, void* stream);
 
 /* --- 2DECOMP transposes ------------------------------------------------------
  * transpose_x_to_y / y_to_z / z_to_y / y_to_x of 2DECOMP&FFT.  On one GPU the

@@ -16,7 +16,7 @@ X3D_OK = 0
 ERRORS = {
     -1: "X3D_ERR_ARG", -2: "X3D_ERR_SHAPE", -3: "X3D_ERR_BC", -4: "X3D_ERR_DTYPE",
     -5: "X3D_ERR_CUDA", -6: "X3D_ERR_COEF", -7: "X3D_ERR_UNSUPPORTED", -8: "X3D_ERR_NOMEM",
-    -9: "X3D_ERR_STATE",
+    -9: "X3D_ERR_STATE", -10: "X3D_ERR_SCRATCH",
 }
 
 OP_DER1, OP_DER2, OP_FIL, OP_DVP, OP_IVP, OP_DPV, OP_IPV = range(7)
@@ -104,6 +104,7 @@ def load():
         lib.x3d_derypv.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, I, I, I, I, I, P]
         lib.x3d_poisson.argtypes = [P, P, P]
         lib.x3d_poisson_ex.argtypes = [P, P, I, P]
+        lib.x3d_poisson_noalloc.argtypes = [P, P, P]
         for n in ("x_to_y", "y_to_z", "z_to_y", "y_to_x"):
             getattr(lib, "x3d_transpose_" + n).argtypes = [P, P, P, LL, P]
         lib.x3d_divergence.argtypes = [P, P, P, P, P, P]

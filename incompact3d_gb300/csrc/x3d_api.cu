@@ -176,6 +176,7 @@ const char* x3d_strerror(int s) {
     case X3D_ERR_UNSUPPORTED: return "option outside the implemented scope";
     case X3D_ERR_NOMEM: return "device allocation failed";
     case X3D_ERR_STATE: return "solver state error";
+    case X3D_ERR_SCRATCH: return "problem larger than the fixed scratch of the allocation-free entry point";
   }
   return "unknown status";
 }
@@ -391,6 +392,10 @@ int x3d_interzpv(x3d_ctx* h, double* tz, const double* uz, double*, double*, con
 int x3d_poisson(x3d_ctx* h, double* rhs, void* st) {
   if (!h || !rhs) return X3D_ERR_ARG;
   return poisson_periodic(C(h), rhs, 0, (cudaStream_t)st);
+}
+int x3d_poisson_noalloc(x3d_ctx* h, double* rhs, void* st) {
+  if (!h || !rhs) return X3D_ERR_ARG;
+  return poisson_periodic_noalloc(C(h), rhs, (cudaStream_t)st);
 }
 int x3d_poisson_ex(x3d_ctx* h, double* rhs, int precision, void* st) {
   if (!h || !rhs) return X3D_ERR_ARG;

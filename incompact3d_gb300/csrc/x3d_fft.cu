@@ -19,6 +19,7 @@
 // decision is bit-identical to the reference's.
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "x3d_internal.h"
@@ -410,6 +411,181 @@ int poisson_periodic(Ctx* c, double* rhs, int precision, cudaStream_t st) {
   if (precision == 0) return poisson_run<double>(c, rhs, st);
   if (precision == 1) return poisson_run<float>(c, rhs, st);
   return X3D_ERR_DTYPE;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free Poisson solve (x3d_poisson_noalloc).
+//
+// Some callers cannot allocate device memory at the point where they solve:
+// codes that reserve the whole device up front in their own memory pool (a
+// caching allocator, or a solver that sizes every buffer at start-up and
+// treats a later allocation as an error), or that call from a context where a
+// cudaMalloc would be refused.  This variant takes its spectrum and its
+// twiddle / wavenumber tables from one fixed array in device memory instead
+// of the context's lazily allocated buffers, and calls no allocating routine.
+//
+// The array below is part of the library's device image: every GPU that
+// loads the library holds these 64 MiB until the process exits.  All calls
+// (from any context, on any stream) share it and it keeps the previous call's
+// contents; each call rewrites the tables and the whole spectrum before
+// reading them, so nothing needs clearing, but two calls that overlap on the
+// GPU race on it.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocBytes = size_t(X3D_NOALLOC_SCRATCH_BYTES);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[64] = {nullptr};
+
+// Device address of the scratch array for the current device.  Host code may
+// not use the symbol's name as an address; the address is fetched once per
+// device (with that device current) and cached.  The first call on a device
+// does this set-up, so it should come before any stream capture.
+int noalloc_scratch(int dev, unsigned char** out) {
+  if (dev < 0 || dev >= 64) return X3D_ERR_ARG;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_status(e);
+    g_noalloc_addr[dev] = p;
+  }
+  *out = static_cast<unsigned char*>(g_noalloc_addr[dev]);
+  return X3D_OK;
+}
+
+struct WaveAxis {
+  int n;
+  double len, d, aci6, bci6, alcai6, aici6, bici6, cici6, dici6, ailcai6;
+};
+
+WaveAxis wave_axis(const AxisCoef& a) {
+  return WaveAxis{a.n, a.len, a.d, a.aci6, a.bci6, a.alcai6, a.aici6, a.bici6, a.cici6s, a.dici6, a.ailcai6};
+}
+
+__device__ void tw_entry(double2* t, int m, int n, double sign) {
+  double s, c;
+  sincospi(2.0 * (double)m / (double)n, &s, &c);
+  *t = double2{c, sign * s};
+}
+
+// Twiddles (same layout as the context's table) and the modified-wavenumber /
+// transfer tables of the periodic waves() branch, written into the scratch.
+__global__ void k_noalloc_tables(double2* tw, double* k2, double* tr, int nx, int ny, int nz, WaveAxis ax,
+                                 WaveAxis ay, WaveAxis az) {
+  const int M = nx / 2;
+  const int ntw = 3 * M + 1 + 2 * ny + 2 * nz;
+  const double twopi = 6.283185307179586476925286766559;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < ntw + nx + ny + nz; q += gridDim.x * blockDim.x) {
+    if (q < ntw) {
+      int m = q;
+      if (m < M) { tw_entry(tw + q, m, M, -1.0); continue; }
+      m -= M;
+      if (m < M) { tw_entry(tw + q, m, M, 1.0); continue; }
+      m -= M;
+      if (m <= M) { tw_entry(tw + q, m, nx, -1.0); continue; }
+      m -= M + 1;
+      if (m < ny) { tw_entry(tw + q, m, ny, -1.0); continue; }
+      m -= ny;
+      if (m < ny) { tw_entry(tw + q, m, ny, 1.0); continue; }
+      m -= ny;
+      if (m < nz) { tw_entry(tw + q, m, nz, -1.0); continue; }
+      m -= nz;
+      tw_entry(tw + q, m, nz, 1.0);
+      continue;
+    }
+    int i = q - ntw;
+    const WaveAxis* a = &ax;
+    int off = 0;
+    if (i >= nx) { i -= nx; off += nx; a = &ay; if (i >= ny) { i -= ny; off += ny; a = &az; } }
+    const int n = a->n;
+    const int ii = (i <= n / 2) ? i : n - i;  // tables are symmetric in the mode index
+    const double w = twopi * ii / n;
+    double wp = a->aci6 * 2.0 * a->d * sin(w * 0.5) + a->bci6 * 2.0 * a->d * sin(3.0 * 0.5 * w);
+    wp = wp / (1.0 + 2.0 * a->alcai6 * cos(w));
+    const double kk = n * wp / a->len;
+    k2[off + i] = kk * kk;
+    const double rl = (n * w / a->len) * a->d;
+    const double tt = 2.0 * (a->bici6 * cos(rl * 1.5) + a->cici6 * cos(rl * 2.5) + a->dici6 * cos(rl * 3.5));
+    const double tt1 = 2.0 * a->aici6 * cos(rl * 0.5);
+    const double t1 = 1.0 + 2.0 * a->ailcai6 * cos(rl);
+    tr[off + i] = (tt1 + tt) / t1;
+  }
+}
+
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+}  // namespace
+
+int poisson_periodic_noalloc(Ctx* c, double* rhs, cudaStream_t st) {
+  typedef double2 C;
+  const int nx = c->grid.nx, ny = c->grid.ny, nz = c->grid.nz;
+  if (!c->ax[0].periodic || !c->ax[1].periodic || !c->ax[2].periodic) return X3D_ERR_BC;
+  if (!pow2(nx) || !pow2(ny) || !pow2(nz) || nx < 16 || ny < 8 || nz < 8) return X3D_ERR_UNSUPPORTED;
+  if (nx / 2 > FFT_ELEMS || ny > FFT_ELEMS || nz > FFT_ELEMS) return X3D_ERR_UNSUPPORTED;
+  const int M = nx / 2, nxh = M + 1;
+  const size_t ntw = (size_t)3 * M + 1 + 2 * ny + 2 * nz;
+  const size_t b_tw = align256(ntw * sizeof(C));
+  const size_t b_tab = align256((size_t)(nx + ny + nz) * sizeof(double));
+  const size_t b_spec = (size_t)nxh * ny * nz * sizeof(C);
+  if (b_tw + 2 * b_tab + b_spec > kNoAllocBytes) return X3D_ERR_SCRATCH;
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (dev != c->device) return X3D_ERR_ARG;
+  unsigned char* base = nullptr;
+  int rc = noalloc_scratch(dev, &base);
+  if (rc != X3D_OK) return rc;
+  C* tw = reinterpret_cast<C*>(base);
+  double* k2 = reinterpret_cast<double*>(base + b_tw);
+  double* tr = reinterpret_cast<double*>(base + b_tw + b_tab);
+  C* spec = reinterpret_cast<C*>(base + b_tw + 2 * b_tab);
+  k_noalloc_tables<<<64, 256, 0, st>>>(tw, k2, tr, nx, ny, nz, wave_axis(c->ax[0]), wave_axis(c->ax[1]),
+                                       wave_axis(c->ax[2]));
+  rc = cuda_status(cudaGetLastError());
+  if (rc != X3D_OK) return rc;
+  const C* twx_f = tw;
+  const C* twx_i = tw + M;
+  const C* twx_full = tw + 2 * M;
+  const C* twy_f = twx_full + nxh;
+  const C* twy_i = twy_f + ny;
+  const C* twz_f = twy_i + ny;
+  const C* twz_i = twz_f + nz;
+  Spec sp;
+  sp.k2[0] = k2; sp.k2[1] = k2 + nx; sp.k2[2] = k2 + nx + ny;
+  sp.tr[0] = tr; sp.tr[1] = tr + nx; sp.tr[2] = tr + nx + ny;
+  sp.nx = nx; sp.ny = ny; sp.nz = nz;
+  sp.scale = 1.0 / ((double)nx * (double)ny * (double)nz);
+  const long long nlines = (long long)ny * nz;
+  const int lpb = std::max(1, FFT_ELEMS / std::max(M, 1));
+  const size_t smem_x = (size_t)lpb * M * sizeof(C);
+  const unsigned nbx = (unsigned)((nlines + lpb - 1) / lpb);
+  const int lanes_y = std::max(1, std::min(32, FFT_ELEMS / ny));
+  const size_t smem_y = (size_t)lanes_y * (ny + 1) * sizeof(C);
+  const int lanes_z = std::max(1, std::min(32, FFT_ELEMS / nz));
+  const size_t smem_z = (size_t)lanes_z * (nz + 1) * sizeof(C);
+  auto kr2c = fft_x_r2c<double>;
+  auto kyf = fft_strided<double, false, -1>;
+  auto kz = fft_strided<double, true, -1>;
+  auto kyi = fft_strided<double, false, 1>;
+  auto kc2r = fft_x_c2r<double>;
+  if ((e = cudaFuncSetAttribute(kr2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(kyf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(kz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_z)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(kyi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(kc2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x)) != cudaSuccess)
+    return cuda_status(e);
+  kr2c<<<nbx, FFT_THREADS, smem_x, st>>>(rhs, spec, nx, nlines, lpb, twx_f, twx_full);
+  kyf<<<dim3((nxh + lanes_y - 1) / lanes_y, nz), FFT_THREADS, smem_y, st>>>(spec, ny, nxh, nxh, lanes_y,
+                                                                           (long long)nxh * ny, twy_f, twy_i, sp);
+  kz<<<dim3((nxh + lanes_z - 1) / lanes_z, ny), FFT_THREADS, smem_z, st>>>(spec, nz, (long long)nxh * ny, nxh,
+                                                                          lanes_z, nxh, twz_f, twz_i, sp);
+  kyi<<<dim3((nxh + lanes_y - 1) / lanes_y, nz), FFT_THREADS, smem_y, st>>>(spec, ny, nxh, nxh, lanes_y,
+                                                                           (long long)nxh * ny, twy_f, twy_i, sp);
+  kc2r<<<nbx, FFT_THREADS, smem_x, st>>>(spec, rhs, nx, nlines, lpb, twx_i, twx_full);
+  return cuda_status(cudaGetLastError());
 }
 
 }  // namespace x3d

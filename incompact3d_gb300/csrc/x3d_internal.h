@@ -130,6 +130,8 @@ int plan_info(Ctx* c, int axis, int kind, int npaire, int coefset, double* sc, d
 
 // Poisson (periodic, all three directions).  precision 0: FP64 FFT, 1: FP32 FFT.
 int poisson_periodic(Ctx* c, double* rhs, int precision, cudaStream_t st);
+// Same solve with all scratch in a fixed device array (no allocation).
+int poisson_periodic_noalloc(Ctx* c, double* rhs, cudaStream_t st);
 
 // Records the CUDA error behind an X3D_ERR_CUDA (see x3d_last_cuda_error).
 void note_cuda_error(cudaError_t e);

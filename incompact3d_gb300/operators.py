@@ -174,6 +174,14 @@ class Context:
         check(self.lib.x3d_poisson_ex(self.h, _ptr(rhs), precision, _stream()), "x3d_poisson")
         return rhs
 
+    def poisson_noalloc(self, rhs):
+        """x3d_poisson_noalloc: same solve as poisson(), with all scratch in the
+        library's fixed device array (no allocation; grids up to its size)."""
+        torch = _torch()
+        _dev(rhs, torch.float64)
+        check(self.lib.x3d_poisson_noalloc(self.h, _ptr(rhs), _stream()), "x3d_poisson_noalloc")
+        return rhs
+
     def divergence(self, ux, uy, uz, pp3=None):
         torch = _torch()
         if pp3 is None:
