@@ -100,6 +100,7 @@ struct Ctx {
   x3d_numopts opts;
   int device = 0;
   int num_sms = 0;
+  bool fast_lines = true;  // FP32 periodic lines of 16*L points use line_fast
   AxisCoef ax[3];
   std::map<int, std::unique_ptr<OpPlan>> plans;  // key = packed (axis,kind,npaire,coefset)
   // Poisson device tables

@@ -1,0 +1,237 @@
+// Fast path of the compact-operator line kernel for periodic lines whose
+// length is 16*L (L = 8, 16 or 32): every chunk is full, so nothing is
+// predicated.  Same algorithm as line_kernel (x3d_line_kernel.cuh) with a
+// leaner instruction stream:
+//   * y/z lines: each thread loads its chunk plus the stencil halo straight
+//     from HBM into a register window (32 consecutive x-points per warp: one
+//     coalesced 128-byte row segment per load); no shared-memory tile.
+//     x lines: the 32 lines are staged once through a padded shared tile (the
+//     transpose), then read into the same register window.
+//   * away from the line ends the LU factors are constant to the last bit
+//     (the pivots of prepare() converge), so those chunks use three scalar
+//     factors and generate the chunk fix-up factors by running products
+//     instead of loading six coefficient vectors per row;
+//   * the Sherman-Morrison correction is applied only to chunks where the
+//     precomputed vector is non-zero in this precision.
+#pragma once
+#include "x3d_line_kernel.cuh"
+
+namespace x3d {
+namespace lk {
+
+constexpr int FCHUNKS = 16;
+
+template <typename T>
+struct FastArgs {
+  const T* in;
+  T* out;
+  long long sa, sb, rs;  // line (a, b) offset and row stride (same for in and out)
+  int n, na;
+  const T *s, *f, *w, *pf, *qb, *rsm;  // per-row vectors (non-uniform chunks)
+  T ca, cb, cc, cd, alpha, den;
+  T s_inf, f_inf, w_inf, g_inf;  // interior factors; g = -(f*w)
+  T pfe[FCHUNKS];                // pf at each chunk's last row
+  T qbs[FCHUNKS];                // qb at each chunk's first row
+  int mode[FCHUNKS];             // bit0: uniform factors, bit1: SM vector non-zero
+  int nterms_int;
+};
+
+template <int KIND>
+struct Halo {
+  static constexpr int lo = -Ext<KIND>::lo, hi = Ext<KIND>::hi;
+};
+
+// Interior stencil on the register window: w[j] holds u[r0 - lo + j].
+template <typename T, int KIND, int LO>
+__device__ __forceinline__ T interior_w(const T* w, int k, const FastArgs<T>& p) {
+#define W_(d) w[k + LO + (d)]
+  if constexpr (KIND == K_DER1) {
+    return p.ca * (W_(1) - W_(-1)) + p.cb * (W_(2) - W_(-2));
+  } else if constexpr (KIND == K_DER2) {
+    const T ur = W_(0);
+    T acc = p.ca * (W_(1) - ur - ur + W_(-1)) + p.cb * (W_(2) - ur - ur + W_(-2));
+    if (p.nterms_int > 2) acc = acc + p.cc * (W_(3) - ur - ur + W_(-3)) + p.cd * (W_(4) - ur - ur + W_(-4));
+    return acc;
+  } else if constexpr (KIND == K_FIL) {
+    return p.ca * W_(0) + p.cb * (W_(1) + W_(-1)) + p.cc * (W_(2) + W_(-2)) + p.cd * (W_(3) + W_(-3));
+  } else if constexpr (KIND == K_DVP) {
+    return p.ca * (W_(1) - W_(0)) + p.cb * (W_(2) - W_(-1));
+  } else if constexpr (KIND == K_IVP) {
+    T acc = p.ca * (W_(1) + W_(0)) + p.cb * (W_(2) + W_(-1)) + p.cc * (W_(3) + W_(-2));
+    if (p.nterms_int > 3) acc = acc + p.cd * (W_(4) + W_(-3));
+    return acc;
+  } else if constexpr (KIND == K_DPV) {
+    return p.ca * (W_(0) - W_(-1)) + p.cb * (W_(1) - W_(-2));
+  } else {
+    T acc = p.ca * (W_(0) + W_(-1)) + p.cb * (W_(1) + W_(-2)) + p.cc * (W_(2) + W_(-3));
+    if (p.nterms_int > 3) acc = acc + p.cd * (W_(3) + W_(-4));
+    return acc;
+  }
+#undef W_
+}
+
+template <typename T, int KIND, bool XL, int L>
+__global__ void __launch_bounds__(LANES* FCHUNKS) line_fast(const __grid_constant__ FastArgs<T> p) {
+  constexpr int LO = Halo<KIND>::lo, HI = Halo<KIND>::hi;
+  constexpr int WN = L + LO + HI;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* cfw = reinterpret_cast<T*>(smem_raw);
+  T* cbw = cfw + FCHUNKS * LANES;
+  T* ends = cbw + FCHUNKS * LANES;
+  T* tile = ends + 2 * LANES;  // x lines only: [n][LD]
+
+  const int lane = threadIdx.x, ch = threadIdx.y;
+  const int n = p.n;
+  const int a0 = blockIdx.x * LANES;
+  const long long b = blockIdx.y;
+  const int nl = min(LANES, p.na - a0);
+  const int r0 = ch * L;
+  const int mode = p.mode[ch];
+
+  // 1. register window u[r0-LO .. r0+L+HI) (periodic wrap)
+  T w[WN];
+  if (!XL) {
+    const bool ok = lane < nl;
+    const T* src = p.in + (ok ? (long long)(a0 + lane) * p.sa : 0) + b * p.sb;
+#pragma unroll
+    for (int j = 0; j < WN; ++j) {
+      int r = r0 - LO + j;
+      r = (r < 0) ? r + n : (r >= n ? r - n : r);
+      w[j] = ok ? src[(long long)r * p.rs] : T(0);
+    }
+  } else {
+    const T* src = p.in + (long long)a0 * p.sa + b * p.sb;
+    for (int l = ch; l < LANES; l += FCHUNKS) {
+      if (l < nl) {
+        for (int r = lane; r < n; r += LANES) tile[r * LD + l] = src[(long long)l * p.sa + r];
+      } else {
+        for (int r = lane; r < n; r += LANES) tile[r * LD + l] = T(0);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < WN; ++j) {
+      int r = r0 - LO + j;
+      r = (r < 0) ? r + n : (r >= n ? r - n : r);
+      w[j] = tile[r * LD + lane];
+    }
+  }
+
+  // 2. right-hand side
+  T v[L];
+#pragma unroll
+  for (int k = 0; k < L; ++k) v[k] = interior_w<T, KIND, LO>(w, k, p);
+
+  // 3. forward elimination + carry scan + fix-up
+  T y = T(0);
+  if (mode & 1) {
+#pragma unroll
+    for (int k = 0; k < L; ++k) { y = v[k] - p.s_inf * y; v[k] = y; }
+  } else {
+#pragma unroll
+    for (int k = 0; k < L; ++k) { y = v[k] - p.s[r0 + k] * y; v[k] = y; }
+  }
+  cfw[ch * LANES + lane] = y;
+  __syncthreads();
+  if (ch > 0) {
+    T cin = T(0);
+    for (int c = 0; c < ch; ++c) cin = cfw[c * LANES + lane] + p.pfe[c] * cin;
+    if (mode & 1) {
+      const T m = -p.s_inf;
+      T P = m;
+#pragma unroll
+      for (int k = 0; k < L; ++k) { v[k] = v[k] + P * cin; P = P * m; }
+    } else {
+#pragma unroll
+      for (int k = 0; k < L; ++k) v[k] = v[k] + p.pf[r0 + k] * cin;
+    }
+  }
+
+  // 4. back substitution + carry scan + fix-up
+  T x = T(0);
+  if (mode & 1) {
+#pragma unroll
+    for (int k = L - 1; k >= 0; --k) { x = (v[k] - p.f_inf * x) * p.w_inf; v[k] = x; }
+  } else {
+#pragma unroll
+    for (int k = L - 1; k >= 0; --k) { x = (v[k] - p.f[r0 + k] * x) * p.w[r0 + k]; v[k] = x; }
+  }
+  cbw[ch * LANES + lane] = x;
+  __syncthreads();
+  if (ch < FCHUNKS - 1) {
+    T cin = T(0);
+    for (int c = FCHUNKS - 1; c > ch; --c) cin = cbw[c * LANES + lane] + p.qbs[c] * cin;
+    if (mode & 1) {
+      T Q = p.g_inf;
+#pragma unroll
+      for (int k = L - 1; k >= 0; --k) { v[k] = v[k] + Q * cin; Q = Q * p.g_inf; }
+    } else {
+#pragma unroll
+      for (int k = 0; k < L; ++k) v[k] = v[k] + p.qb[r0 + k] * cin;
+    }
+  }
+
+  // 5. Sherman-Morrison
+  if (ch == 0) ends[lane] = v[0];
+  if (ch == FCHUNKS - 1) ends[LANES + lane] = v[L - 1];
+  __syncthreads();
+  if (mode & 2) {
+    const T sx = (ends[lane] - p.alpha * ends[LANES + lane]) / p.den;
+#pragma unroll
+    for (int k = 0; k < L; ++k) v[k] = v[k] - sx * p.rsm[r0 + k];
+  }
+
+  // 6. store
+  if (!XL) {
+    if (lane < nl) {
+      T* dst = p.out + (long long)(a0 + lane) * p.sa + b * p.sb;
+#pragma unroll
+      for (int k = 0; k < L; ++k) dst[(long long)(r0 + k) * p.rs] = v[k];
+    }
+  } else {
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < L; ++k) tile[(r0 + k) * LD + lane] = v[k];
+    __syncthreads();
+    T* dst = p.out + (long long)a0 * p.sa + b * p.sb;
+    for (int l = ch; l < nl; l += FCHUNKS)
+      for (int r = lane; r < n; r += LANES) dst[(long long)l * p.sa + r] = tile[r * LD + l];
+  }
+}
+
+template <typename T>
+size_t fast_smem(int n, bool xl) {
+  return sizeof(T) * ((size_t)2 * FCHUNKS * LANES + 2 * LANES + (xl ? (size_t)n * LD : 0));
+}
+
+template <typename T, int KIND, bool XL, int L>
+int launch_fast_k(const FastArgs<T>& a, dim3 grid, size_t smem, cudaStream_t st) {
+  auto kern = line_fast<T, KIND, XL, L>;
+  static size_t configured = 0;
+  if (smem > configured) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e);
+    configured = smem;
+  }
+  kern<<<grid, dim3(LANES, FCHUNKS), smem, st>>>(a);
+  return cuda_status(cudaGetLastError());
+}
+
+template <typename T, int KIND>
+int fast_dispatch_xl(const FastArgs<T>& a, bool xl, int L, dim3 grid, size_t smem, cudaStream_t st) {
+  if (xl) {
+    if (L == 8) return launch_fast_k<T, KIND, true, 8>(a, grid, smem, st);
+    if (L == 16) return launch_fast_k<T, KIND, true, 16>(a, grid, smem, st);
+    return launch_fast_k<T, KIND, true, 32>(a, grid, smem, st);
+  }
+  if (L == 8) return launch_fast_k<T, KIND, false, 8>(a, grid, smem, st);
+  if (L == 16) return launch_fast_k<T, KIND, false, 16>(a, grid, smem, st);
+  return launch_fast_k<T, KIND, false, 32>(a, grid, smem, st);
+}
+
+// Instantiated per operator kind in x3d_lines_<kind>.cu (FP32 only).
+template <int KIND>
+int fast_dispatch(const FastArgs<float>& a, bool xl, int L, dim3 grid, size_t smem, cudaStream_t st);
+
+}  // namespace lk
+}  // namespace x3d

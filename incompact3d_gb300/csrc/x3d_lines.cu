@@ -1,7 +1,9 @@
 // Host launcher of the generic compact-operator line kernel
 // (x3d_line_kernel.cuh): per-operator plan finalisation (chunk fix-up
 // factors, device upload) and argument marshalling.
-#include "x3d_line_kernel.cuh"
+#include <type_traits>
+
+#include "x3d_line_fast.cuh"
 
 namespace x3d {
 
@@ -21,6 +23,70 @@ int dispatch(const LineArgs<T>& a, int kind, bool xl, int lmax, dim3 grid, size_
     case K_IPV: return line_dispatch<K_IPV>(a, xl, lmax, grid, smem, st);
   }
   return X3D_ERR_ARG;
+}
+
+int fdispatch(const FastArgs<float>& a, int kind, bool xl, int L, dim3 grid, size_t smem, cudaStream_t st) {
+  switch (kind) {
+    case K_DER1: return fast_dispatch<K_DER1>(a, xl, L, grid, smem, st);
+    case K_DER2: return fast_dispatch<K_DER2>(a, xl, L, grid, smem, st);
+    case K_FIL: return fast_dispatch<K_FIL>(a, xl, L, grid, smem, st);
+    case K_DVP: return fast_dispatch<K_DVP>(a, xl, L, grid, smem, st);
+    case K_IVP: return fast_dispatch<K_IVP>(a, xl, L, grid, smem, st);
+    case K_DPV: return fast_dispatch<K_DPV>(a, xl, L, grid, smem, st);
+    case K_IPV: return fast_dispatch<K_IPV>(a, xl, L, grid, smem, st);
+  }
+  return X3D_ERR_ARG;
+}
+
+// Periodic lines of 16*L points (L = 8, 16, 32) in FP32 take the fast path.
+int launch_fast(OpPlan* p, float* out, const float* in, const int* dims_in, cudaStream_t st) {
+  const int n = p->nout;
+  const int L = n / FCHUNKS;
+  FastArgs<float> a;
+  std::memset(&a, 0, sizeof(a));
+  a.in = in;
+  a.out = out;
+  a.n = n;
+  const long long nx = dims_in[0], ny = dims_in[1], nz = dims_in[2];
+  dim3 grid;
+  const bool xl = (p->axis == 0);
+  if (p->axis == 0) {
+    a.na = (int)ny; a.sa = n; a.sb = ny * n; a.rs = 1;
+    grid = dim3((unsigned)((ny + LANES - 1) / LANES), (unsigned)nz);
+  } else if (p->axis == 1) {
+    a.na = (int)nx; a.sa = 1; a.sb = nx * n; a.rs = nx;
+    grid = dim3((unsigned)((nx + LANES - 1) / LANES), (unsigned)nz);
+  } else {
+    a.na = (int)nx; a.sa = 1; a.sb = nx; a.rs = nx * ny;
+    grid = dim3((unsigned)((nx + LANES - 1) / LANES), (unsigned)ny);
+  }
+  if (grid.y > 65535) return X3D_ERR_UNSUPPORTED;
+  const float* dv = p->dev32;
+  a.s = dv; a.f = dv + n; a.w = dv + 2 * n; a.pf = dv + 3 * n; a.qb = dv + 4 * n; a.rsm = dv + 5 * n;
+  a.ca = (float)p->ca; a.cb = (float)p->cb; a.cc = (float)p->cc; a.cd = (float)p->cd;
+  a.alpha = (float)p->alpha;
+  a.den = (float)p->den;
+  a.nterms_int = 4;
+  if (p->kind == K_DER2 && p->cc == 0.0 && p->cd == 0.0) a.nterms_int = 2;
+  if ((p->kind == K_IVP || p->kind == K_IPV) && p->cd == 0.0) a.nterms_int = 3;
+  const int mid = n / 2;
+  a.s_inf = (float)p->s[mid];
+  a.f_inf = (float)p->f[mid];
+  a.w_inf = (float)p->w[mid];
+  a.g_inf = (float)(-(p->f[mid] * p->w[mid]));
+  for (int c = 0; c < FCHUNKS; ++c) {
+    const int s0 = c * L, e0 = s0 + L - 1;
+    a.pfe[c] = (float)p->pf[e0];
+    a.qbs[c] = (float)p->qb[s0];
+    bool uni = true, sm = false;
+    for (int r = s0; r <= e0; ++r) {
+      uni = uni && (float)p->s[r] == a.s_inf && (float)p->f[r] == a.f_inf && (float)p->w[r] == a.w_inf;
+      sm = sm || (float)p->rsm[r] != 0.0f;
+    }
+    a.mode[c] = (uni ? 1 : 0) | (sm ? 2 : 0);
+  }
+  const size_t smem = fast_smem<float>(n, xl);
+  return fdispatch(a, p->kind, xl, L, grid, smem, st);
 }
 
 template <typename T>
@@ -89,11 +155,13 @@ static int upload_plan(OpPlan* p) {
 
 template <typename T>
 int launch_line_op(Ctx* c, OpPlan* p, T* out, const T* in, const int* dims_in, const T* pp, cudaStream_t st) {
-  (void)c;
   if (!out || !in) return X3D_ERR_ARG;
   if (dims_in[p->axis] != p->nin) return X3D_ERR_SHAPE;
   const int up = upload_plan(p);
   if (up != X3D_OK) return up;
+  if (std::is_same<T, float>::value && p->periodic && p->nin == p->nout && pp == nullptr && c->fast_lines &&
+      p->nout % FCHUNKS == 0 && (p->nout / FCHUNKS == 8 || p->nout / FCHUNKS == 16 || p->nout / FCHUNKS == 32))
+    return launch_fast(p, (float*)out, (const float*)in, dims_in, st);
   LineArgs<T> a;
   std::memset(&a, 0, sizeof(a));
   a.in = in;

@@ -1,6 +1,6 @@
-// Instantiations of the line kernel for one operator kind (K_DER2); split
+// Instantiations of the line kernels for one operator kind (K_DER2); split
 // out so the kernel variants compile in parallel.
-#include "x3d_line_kernel.cuh"
+#include "x3d_line_fast.cuh"
 
 namespace x3d {
 namespace lk {
@@ -11,6 +11,10 @@ int line_dispatch<K_DER2>(const LineArgs<double>& a, bool xl, int lmax, dim3 gri
 template <>
 int line_dispatch<K_DER2>(const LineArgs<float>& a, bool xl, int lmax, dim3 grid, size_t smem, cudaStream_t st) {
   return dispatch_xl<float, K_DER2>(a, xl, lmax, grid, smem, st);
+}
+template <>
+int fast_dispatch<K_DER2>(const FastArgs<float>& a, bool xl, int L, dim3 grid, size_t smem, cudaStream_t st) {
+  return fast_dispatch_xl<float, K_DER2>(a, xl, L, grid, smem, st);
 }
 }  // namespace lk
 }  // namespace x3d

@@ -139,3 +139,22 @@ def test_full_size_512_sampled_lines(oracle_mod, gpu_lib):
             assert relerr(go.cpu().numpy(), ref) < 1e-12, (kind, axis)
     del u
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("n", [128, 256, 512])
+def test_fp32_fast_path_periodic(oracle_mod, gpu_lib, n):
+    """FP32 periodic lines of 16*L points (L = 8, 16, 32) run the register-window
+    fast path (line_fast); every operator kind on every axis vs the oracle."""
+    import torch
+    L = 2 * np.pi
+    for axis in range(3):
+        dims = [24, 20, 18]
+        dims[axis] = n
+        ctx = gpu_lib.Context(*dims, L, L, L, filter_alpha=0.45)
+        o = oracle_mod.Oracle(*dims, L, L, L, filter_alpha=0.45)
+        u = fourier_field(*dims, seed=n + axis, kmax=6)
+        ud = torch.from_numpy(u).to(device="cuda", dtype=torch.float32)
+        for kind in range(7):
+            ref = o.op(axis, kind, 1, u)
+            got = ctx.apply(axis, kind, 1, ud).double().cpu().numpy()
+            assert relerr(got, ref) < 1e-4, (n, axis, OPS[kind], relerr(got, ref))
