@@ -208,7 +208,9 @@ int x3d_filz_f32(x3d_ctx* ctx, float* tz, const float* uz, int nx, int ny, int n
 /* --- Poisson solve ------------------------------------------------------------
  * poisson(rhs) procedure pointer, src/poisson.f90:57-62; all-periodic solver
  * poisson_000, src/poisson.f90:298-410.  rhs (nxm,nym,nzm) in device memory is
- * overwritten by the solution.  precision: 0 = FP64 FFT, 1 = FP32 FFT. */
+ * overwritten by the solution.  precision: 0 = FP64 FFT, 1 = FP32 FFT,
+ * 2 = double-float FFT (each real carried as a hi+lo pair of binary32,
+ * ~48-bit significand, computed on the FP32 pipes). */
 int x3d_poisson(x3d_ctx* ctx, double* rhs, void* stream);
 int x3d_poisson_ex(x3d_ctx* ctx, double* rhs, int precision, void* stream);
 

@@ -16,9 +16,12 @@ Ctx::~Ctx() {
   for (int a = 0; a < 3; ++a) {
     if (d_k2[a]) cudaFree(d_k2[a]);
     if (d_tr[a]) cudaFree(d_tr[a]);
+    if (d_k2df[a]) cudaFree(d_k2df[a]);
+    if (d_trdf[a]) cudaFree(d_trdf[a]);
   }
   if (d_twid) cudaFree(d_twid);
   if (d_twid32) cudaFree(d_twid32);
+  if (d_twid_df) cudaFree(d_twid_df);
   if (fft_work) cudaFree(fft_work);
 }
 

@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "x3d_internal.h"
@@ -32,64 +33,168 @@ constexpr int FFT_THREADS = 512;
 constexpr int FFT_VALS = 8;  // complex values held per thread per pass
 constexpr int FFT_ELEMS = FFT_THREADS * FFT_VALS;  // complex values per CTA
 
-template <typename R>
-struct Cx;
-template <>
-struct Cx<double> { typedef double2 T; };
-template <>
-struct Cx<float> { typedef float2 T; };
+// ---------------------------------------------------------------------------
+// Arithmetic policies.  double / float: native complex arithmetic.  DF: every
+// real number is an unevaluated sum hi + lo of two binary32 numbers (about a
+// 48-bit significand), added with the error-free two-sum and multiplied with
+// the FMA two-product, so FP64-class transforms run on GB300's FP32 pipes
+// (its FP64 pipe is 1/64 of the FP32 rate).  A DF complex is 16 bytes, the
+// size of a double2, so buffers and shared-memory tiles are unchanged.
+// ---------------------------------------------------------------------------
+struct DF {};
+struct df { float h, l; };
+struct __align__(16) cdf { float rh, rl, ih, il; };
 
-template <typename C>
-__device__ __forceinline__ C cadd(C a, C b) { return C{a.x + b.x, a.y + b.y}; }
-template <typename C>
-__device__ __forceinline__ C csub(C a, C b) { return C{a.x - b.x, a.y - b.y}; }
-template <typename C>
-__device__ __forceinline__ C cmul(C a, C b) { return C{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
-// multiply by -i (forward) or +i (inverse)
-template <int SIGN, typename C>
-__device__ __forceinline__ C mul_mi(C a) {
-  if (SIGN < 0) return C{a.y, -a.x};
-  return C{-a.y, a.x};
+__device__ __forceinline__ df two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float v = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v));
+  return df{s, e};
+}
+__device__ __forceinline__ df fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return df{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+  const df s = two_sum(a.h, b.h);
+  return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ df df_neg(df a) { return df{-a.h, -a.l}; }
+__device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ df df_mul(df a, df b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ df df_half(df a) { return df{0.5f * a.h, 0.5f * a.l}; }  // exact
+__device__ __forceinline__ df df_from(double d) {
+  const float h = __double2float_rn(d);
+  return df{h, __double2float_rn(d - (double)h)};
+}
+__device__ __forceinline__ double df_to(df a) { return (double)a.h + (double)a.l; }
+// 1/b with one Newton step in DF
+__device__ __forceinline__ df df_rcp(df b) {
+  const float r0 = 1.0f / b.h;
+  const df br = df_mul(b, df{r0, 0.0f});
+  const df e = df_sub(df{1.0f, 0.0f}, br);
+  return df_add(df{r0, 0.0f}, df_mul(df{r0, 0.0f}, e));
 }
 
-template <int SIGN, typename C>
+template <typename R>
+struct FT;
+
+template <typename R>
+struct FTnative {
+  typedef typename std::conditional<std::is_same<R, double>::value, double2, float2>::type C;
+  static __device__ __forceinline__ C add(C a, C b) { return C{a.x + b.x, a.y + b.y}; }
+  static __device__ __forceinline__ C sub(C a, C b) { return C{a.x - b.x, a.y - b.y}; }
+  static __device__ __forceinline__ C mul(C a, C b) { return C{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+  static __device__ __forceinline__ C conj(C a) { return C{a.x, -a.y}; }
+  static __device__ __forceinline__ C half(C a) { return C{a.x * (R)0.5, a.y * (R)0.5}; }
+  template <int S>
+  static __device__ __forceinline__ C mul_i(C a) {  // a * (S*i)
+    return S < 0 ? C{a.y, -a.x} : C{-a.y, a.x};
+  }
+  template <int S>
+  static __device__ __forceinline__ C w8_1(C o) {
+    const R h = (R)0.70710678118654752440084436210484903928;
+    return S < 0 ? C{(o.x + o.y) * h, (o.y - o.x) * h} : C{(o.x - o.y) * h, (o.y + o.x) * h};
+  }
+  template <int S>
+  static __device__ __forceinline__ C w8_3(C o) {
+    const R h = (R)0.70710678118654752440084436210484903928;
+    return S < 0 ? C{(o.y - o.x) * h, -(o.x + o.y) * h} : C{-(o.x + o.y) * h, (o.x - o.y) * h};
+  }
+  static __device__ __forceinline__ C from(double re, double im) { return C{(R)re, (R)im}; }
+  static __device__ __forceinline__ double re(C a) { return (double)a.x; }
+  static __device__ __forceinline__ double im(C a) { return (double)a.y; }
+  static __device__ __forceinline__ C zero() { return C{(R)0, (R)0}; }
+};
+template <>
+struct FT<double> : FTnative<double> {};
+template <>
+struct FT<float> : FTnative<float> {};
+
+template <>
+struct FT<DF> {
+  typedef cdf C;
+  static __device__ __forceinline__ df R_(C a) { return df{a.rh, a.rl}; }
+  static __device__ __forceinline__ df I_(C a) { return df{a.ih, a.il}; }
+  static __device__ __forceinline__ C mk(df r, df i) { return C{r.h, r.l, i.h, i.l}; }
+  static __device__ __forceinline__ C add(C a, C b) { return mk(df_add(R_(a), R_(b)), df_add(I_(a), I_(b))); }
+  static __device__ __forceinline__ C sub(C a, C b) { return mk(df_sub(R_(a), R_(b)), df_sub(I_(a), I_(b))); }
+  static __device__ __forceinline__ C mul(C a, C b) {
+    return mk(df_sub(df_mul(R_(a), R_(b)), df_mul(I_(a), I_(b))), df_add(df_mul(R_(a), I_(b)), df_mul(I_(a), R_(b))));
+  }
+  static __device__ __forceinline__ C conj(C a) { return C{a.rh, a.rl, -a.ih, -a.il}; }
+  static __device__ __forceinline__ C half(C a) { return mk(df_half(R_(a)), df_half(I_(a))); }
+  template <int S>
+  static __device__ __forceinline__ C mul_i(C a) {
+    return S < 0 ? C{a.ih, a.il, -a.rh, -a.rl} : C{-a.ih, -a.il, a.rh, a.rl};
+  }
+  static __device__ __forceinline__ df h_() { return df{0.70710677f, 1.2101617e-08f}; }  // 1/sqrt(2) as hi+lo
+  template <int S>
+  static __device__ __forceinline__ C w8_1(C o) {
+    const df x = R_(o), y = I_(o), h = h_();
+    return S < 0 ? mk(df_mul(df_add(x, y), h), df_mul(df_sub(y, x), h))
+                 : mk(df_mul(df_sub(x, y), h), df_mul(df_add(y, x), h));
+  }
+  template <int S>
+  static __device__ __forceinline__ C w8_3(C o) {
+    const df x = R_(o), y = I_(o), h = h_();
+    return S < 0 ? mk(df_mul(df_sub(y, x), h), df_neg(df_mul(df_add(x, y), h)))
+                 : mk(df_neg(df_mul(df_add(x, y), h)), df_mul(df_sub(x, y), h));
+  }
+  static __device__ __forceinline__ C from(double re, double im) { return mk(df_from(re), df_from(im)); }
+  static __device__ __forceinline__ double re(C a) { return df_to(R_(a)); }
+  static __device__ __forceinline__ double im(C a) { return df_to(I_(a)); }
+  static __device__ __forceinline__ C zero() { return C{0.f, 0.f, 0.f, 0.f}; }
+};
+
+template <typename P>
+struct Cx {
+  typedef typename FT<P>::C T;
+};
+
+template <int SIGN, typename P, typename C>
 __device__ __forceinline__ void fft2(C& a, C& b) {
   C t = a;
-  a = cadd(t, b);
-  b = csub(t, b);
+  a = FT<P>::add(t, b);
+  b = FT<P>::sub(t, b);
 }
 
-template <int SIGN, typename C>
+template <int SIGN, typename P, typename C>
 __device__ __forceinline__ void fft4(C& x0, C& x1, C& x2, C& x3) {
-  C s02 = cadd(x0, x2), d02 = csub(x0, x2);
-  C s13 = cadd(x1, x3), d13 = mul_mi<SIGN>(csub(x1, x3));
-  x0 = cadd(s02, s13);
-  x2 = csub(s02, s13);
-  x1 = cadd(d02, d13);
-  x3 = csub(d02, d13);
+  typedef FT<P> F;
+  C s02 = F::add(x0, x2), d02 = F::sub(x0, x2);
+  C s13 = F::add(x1, x3), d13 = F::template mul_i<SIGN>(F::sub(x1, x3));
+  x0 = F::add(s02, s13);
+  x2 = F::sub(s02, s13);
+  x1 = F::add(d02, d13);
+  x3 = F::sub(d02, d13);
 }
 
-template <int SIGN, typename C>
+template <int SIGN, typename P, typename C>
 __device__ __forceinline__ void fft8(C* v) {
-  typedef decltype(v[0].x) R;
-  const R h = (R)0.70710678118654752440084436210484903928;
+  typedef FT<P> F;
   C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
   C o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
-  fft4<SIGN>(e0, e1, e2, e3);
-  fft4<SIGN>(o0, o1, o2, o3);
-  // o_k *= W8^(SIGN k)
-  C t1 = (SIGN < 0) ? C{(o1.x + o1.y) * h, (o1.y - o1.x) * h} : C{(o1.x - o1.y) * h, (o1.y + o1.x) * h};
-  C t2 = mul_mi<SIGN>(o2);
-  C t3 = (SIGN < 0) ? C{(o3.y - o3.x) * h, -(o3.x + o3.y) * h} : C{-(o3.x + o3.y) * h, (o3.x - o3.y) * h};
-  v[0] = cadd(e0, o0); v[4] = csub(e0, o0);
-  v[1] = cadd(e1, t1); v[5] = csub(e1, t1);
-  v[2] = cadd(e2, t2); v[6] = csub(e2, t2);
-  v[3] = cadd(e3, t3); v[7] = csub(e3, t3);
+  fft4<SIGN, P>(e0, e1, e2, e3);
+  fft4<SIGN, P>(o0, o1, o2, o3);
+  C t1 = F::template w8_1<SIGN>(o1);
+  C t2 = F::template mul_i<SIGN>(o2);
+  C t3 = F::template w8_3<SIGN>(o3);
+  v[0] = F::add(e0, o0); v[4] = F::sub(e0, o0);
+  v[1] = F::add(e1, t1); v[5] = F::sub(e1, t1);
+  v[2] = F::add(e2, t2); v[6] = F::sub(e2, t2);
+  v[3] = F::add(e3, t3); v[7] = F::sub(e3, t3);
 }
 
 // One Stockham pass of radix R over `nl` lines of length n held in smem
 // (line l at buf + l*lstride).  tw[m] = exp(SIGN*2*pi*i*m/n).
-template <int R, int SIGN, typename C>
+template <int R, int SIGN, typename P, typename C>
 __device__ __forceinline__ void stockham_pass(C* buf, int lstride, int n, int nl, int Ns, const C* tw) {
   constexpr int G = FFT_VALS / R;  // butterflies per thread
   const int per_line = n / R;
@@ -108,12 +213,12 @@ __device__ __forceinline__ void stockham_pass(C* buf, int lstride, int n, int nl
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         C x = line[j + r * per_line];
-        if (r > 0 && kk > 0) x = cmul(x, tw[(kk * r * step) % n]);
+        if (r > 0 && kk > 0) x = FT<P>::mul(x, tw[(kk * r * step) % n]);
         v[g][r] = x;
       }
-      if (R == 8) fft8<SIGN>(v[g]);
-      if (R == 4) fft4<SIGN>(v[g][0], v[g][1], v[g][2], v[g][3]);
-      if (R == 2) fft2<SIGN>(v[g][0], v[g][1]);
+      if (R == 8) fft8<SIGN, P>(v[g]);
+      if (R == 4) fft4<SIGN, P>(v[g][0], v[g][1], v[g][2], v[g][3]);
+      if (R == 2) fft2<SIGN, P>(v[g][0], v[g][1]);
       base[g] = l * lstride + (j / Ns) * Ns * R + kk;
     }
   }
@@ -127,55 +232,56 @@ __device__ __forceinline__ void stockham_pass(C* buf, int lstride, int n, int nl
   __syncthreads();
 }
 
-template <int SIGN, typename C>
+template <int SIGN, typename P, typename C>
 __device__ void smem_fft(C* buf, int lstride, int n, int nl, const C* tw) {
   int Ns = 1;
   int rem = n;
-  while (rem >= 8) { stockham_pass<8, SIGN>(buf, lstride, n, nl, Ns, tw); Ns *= 8; rem /= 8; }
-  if (rem == 4) { stockham_pass<4, SIGN>(buf, lstride, n, nl, Ns, tw); Ns *= 4; rem /= 4; }
-  if (rem == 2) { stockham_pass<2, SIGN>(buf, lstride, n, nl, Ns, tw); }
+  while (rem >= 8) { stockham_pass<8, SIGN, P>(buf, lstride, n, nl, Ns, tw); Ns *= 8; rem /= 8; }
+  if (rem == 4) { stockham_pass<4, SIGN, P>(buf, lstride, n, nl, Ns, tw); Ns *= 4; rem /= 4; }
+  if (rem == 2) { stockham_pass<2, SIGN, P>(buf, lstride, n, nl, Ns, tw); }
 }
 
 // ---- Pass A: x real-to-complex --------------------------------------------
 // Lines of nx reals -> nx/2+1 complex.  M = nx/2, packed z[m] = x[2m] + i x[2m+1].
-template <typename R>
+template <typename P>
 __global__ void __launch_bounds__(FFT_THREADS) fft_x_r2c(const double* __restrict__ in,
-                                                         typename Cx<R>::T* __restrict__ out, int nx, long long nlines,
-                                                         int lpb, const typename Cx<R>::T* __restrict__ tw_half,
-                                                         const typename Cx<R>::T* __restrict__ tw_full) {
-  typedef typename Cx<R>::T C;
+                                                         typename Cx<P>::T* __restrict__ out, int nx, long long nlines,
+                                                         int lpb, const typename Cx<P>::T* __restrict__ tw_half,
+                                                         const typename Cx<P>::T* __restrict__ tw_full) {
+  typedef typename Cx<P>::T C;
+  typedef FT<P> F;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
   const int M = nx / 2, nxh = M + 1;
   const long long l0 = (long long)blockIdx.x * lpb;
   const int nl = (int)min((long long)lpb, nlines - l0);
-  const double* src = in + l0 * nx;
+  const double2* src = reinterpret_cast<const double2*>(in + l0 * nx);
   for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
-    const int l = e / M, m = e - l * M;
-    buf[l * M + m] = C{(R)src[(long long)l * nx + 2 * m], (R)src[(long long)l * nx + 2 * m + 1]};
+    const double2 d = src[e];  // (x[2m], x[2m+1]) of line e / M
+    buf[e] = F::from(d.x, d.y);
   }
   __syncthreads();
-  smem_fft<-1>(buf, M, M, nl, tw_half);
+  smem_fft<-1, P>(buf, M, M, nl, tw_half);
   C* dst = out + l0 * nxh;
   for (int e = threadIdx.x; e < nl * nxh; e += FFT_THREADS) {
     const int l = e / nxh, k = e - l * nxh;
     const C* z = buf + l * M;
-    const C zk = z[k % M], zn = z[(M - k) % M];
+    const C zk = z[k % M], zn = F::conj(z[(M - k) % M]);
     // E = (Z[k] + conj Z[M-k])/2, O = (Z[k] - conj Z[M-k])/(2i), X = E + W^k O
-    const C E = C{(zk.x + zn.x) * (R)0.5, (zk.y - zn.y) * (R)0.5};
-    const C O = C{(zk.y + zn.y) * (R)0.5, -(zk.x - zn.x) * (R)0.5};
-    const C X = cadd(E, cmul(tw_full[k], O));
-    dst[(long long)l * nxh + k] = X;
+    const C E = F::half(F::add(zk, zn));
+    const C O = F::half(F::template mul_i<-1>(F::sub(zk, zn)));
+    dst[(long long)l * nxh + k] = F::add(E, F::mul(tw_full[k], O));
   }
 }
 
 // ---- Pass E: x complex-to-real (unnormalised inverse) ----------------------
-template <typename R>
-__global__ void __launch_bounds__(FFT_THREADS) fft_x_c2r(const typename Cx<R>::T* __restrict__ in,
+template <typename P>
+__global__ void __launch_bounds__(FFT_THREADS) fft_x_c2r(const typename Cx<P>::T* __restrict__ in,
                                                          double* __restrict__ out, int nx, long long nlines, int lpb,
-                                                         const typename Cx<R>::T* __restrict__ tw_half_inv,
-                                                         const typename Cx<R>::T* __restrict__ tw_full) {
-  typedef typename Cx<R>::T C;
+                                                         const typename Cx<P>::T* __restrict__ tw_half_inv,
+                                                         const typename Cx<P>::T* __restrict__ tw_full) {
+  typedef typename Cx<P>::T C;
+  typedef FT<P> F;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
   const int M = nx / 2, nxh = M + 1;
@@ -185,22 +291,18 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_x_c2r(const typename Cx<R>::T
   for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
     const int l = e / M, k = e - l * M;
     const C xk = src[(long long)l * nxh + k];
-    const C xn = src[(long long)l * nxh + (M - k)];
+    const C xn = F::conj(src[(long long)l * nxh + (M - k)]);
     // E = X[k] + conj X[M-k]; O = (X[k] - conj X[M-k]) * conj(W^k); Z = E + i O
-    const C E = C{xk.x + xn.x, xk.y - xn.y};
-    const C D = C{xk.x - xn.x, xk.y + xn.y};
-    const C w = tw_full[k];
-    const C O = C{D.x * w.x + D.y * w.y, D.y * w.x - D.x * w.y};
-    buf[l * M + k] = C{E.x - O.y, E.y + O.x};
+    const C E = F::add(xk, xn);
+    const C O = F::mul(F::sub(xk, xn), F::conj(tw_full[k]));
+    buf[l * M + k] = F::add(E, F::template mul_i<1>(O));
   }
   __syncthreads();
-  smem_fft<1>(buf, M, M, nl, tw_half_inv);
-  double* dst = out + l0 * nx;
+  smem_fft<1, P>(buf, M, M, nl, tw_half_inv);
+  double2* dst = reinterpret_cast<double2*>(out + l0 * nx);
   for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
-    const int l = e / M, m = e - l * M;
-    const C z = buf[l * M + m];
-    dst[(long long)l * nx + 2 * m] = (double)z.x;
-    dst[(long long)l * nx + 2 * m + 1] = (double)z.y;
+    const C z = buf[e];
+    dst[e] = double2{F::re(z), F::im(z)};
   }
 }
 
@@ -210,16 +312,61 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_x_c2r(const typename Cx<R>::T
 struct Spec {
   const double* k2[3];
   const double* tr[3];
+  const float2* k2df[3];  // hi/lo split of k2 / tr (DF policy)
+  const float2* trdf[3];
   int nx, ny, nz;
   double scale;  // 1/(nx*ny*nz)
 };
 
-template <typename R, bool POISSON, int SIGN>
-__global__ void __launch_bounds__(FFT_THREADS) fft_strided(typename Cx<R>::T* __restrict__ data, int n, long long rs,
+// K of poisson_000's kxyz (src/poisson.f90:1688-1724, periodic): unfused IEEE
+// binary64 in the reference's order, so the zeroing decision is the reference's.
+__device__ __forceinline__ double kxyz64(const Spec& sp, int kx, int ky, int kz) {
+  const double tx = sp.tr[0][kx], ty = sp.tr[1][ky], tz = sp.tr[2][kz];
+  const double pyz = __dmul_rn(ty, tz), pxz = __dmul_rn(tx, tz), pxy = __dmul_rn(tx, ty);
+  return __dadd_rn(__dadd_rn(__dmul_rn(sp.k2[0][kx], __dmul_rn(pyz, pyz)), __dmul_rn(sp.k2[1][ky], __dmul_rn(pxz, pxz))),
+                   __dmul_rn(sp.k2[2][kz], __dmul_rn(pxy, pxy)));
+}
+
+template <typename P>
+struct Spectral {
+  // v / (-K nx ny nz), or 0 where K < 1e-16
+  static __device__ __forceinline__ typename Cx<P>::T apply(typename Cx<P>::T v, const Spec& sp, int kx, int ky,
+                                                            int kz) {
+    typedef typename Cx<P>::T C;
+    const double kk = kxyz64(sp, kx, ky, kz);
+    if (kk < 1.0e-16) return FT<P>::zero();
+    const double f = -sp.scale / kk;
+    return C{(decltype(v.x))(v.x * f), (decltype(v.y))(v.y * f)};
+  }
+};
+
+template <>
+struct Spectral<DF> {
+  static __device__ __forceinline__ cdf apply(cdf v, const Spec& sp, int kx, int ky, int kz) {
+    const float2 tx2 = sp.trdf[0][kx], ty2 = sp.trdf[1][ky], tz2 = sp.trdf[2][kz];
+    const float2 ax = sp.k2df[0][kx], ay = sp.k2df[1][ky], az = sp.k2df[2][kz];
+    const df tx{tx2.x, tx2.y}, ty{ty2.x, ty2.y}, tz{tz2.x, tz2.y};
+    const df pyz = df_mul(ty, tz), pxz = df_mul(tx, tz), pxy = df_mul(tx, ty);
+    df kk = df_add(df_add(df_mul(df{ax.x, ax.y}, df_mul(pyz, pyz)), df_mul(df{ay.x, ay.y}, df_mul(pxz, pxz))),
+                   df_mul(df{az.x, az.y}, df_mul(pxy, pxy)));
+    if (kk.h < 1.0e-12f) {
+      // near the zeroing threshold: decide and scale from the exact binary64 K
+      const double k64 = kxyz64(sp, kx, ky, kz);
+      if (k64 < 1.0e-16) return cdf{0.f, 0.f, 0.f, 0.f};
+      kk = df_from(k64);
+    }
+    const df sc = df_from(-sp.scale);  // uniform; one conversion per mode
+    const df f = df_mul(sc, df_rcp(kk));
+    return FT<DF>::mk(df_mul(FT<DF>::R_(v), f), df_mul(FT<DF>::I_(v), f));
+  }
+};
+
+template <typename P, bool POISSON, int SIGN>
+__global__ void __launch_bounds__(FFT_THREADS) fft_strided(typename Cx<P>::T* __restrict__ data, int n, long long rs,
                                                            int na, int lanes, long long bs,
-                                                           const typename Cx<R>::T* __restrict__ tw_f,
-                                                           const typename Cx<R>::T* __restrict__ tw_i, Spec sp) {
-  typedef typename Cx<R>::T C;
+                                                           const typename Cx<P>::T* __restrict__ tw_f,
+                                                           const typename Cx<P>::T* __restrict__ tw_i, Spec sp) {
+  typedef typename Cx<P>::T C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
   const int lstride = n + 1;
@@ -232,29 +379,15 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_strided(typename Cx<R>::T* __
     if (l < nl) buf[l * lstride + r] = base[r * rs + l];
   }
   __syncthreads();
-  smem_fft<SIGN>(buf, lstride, n, nl, SIGN < 0 ? tw_f : tw_i);
+  smem_fft<SIGN, P>(buf, lstride, n, nl, SIGN < 0 ? tw_f : tw_i);
   if (POISSON) {
     // z-lines: a = kx (0..nx/2), b = ky; row r = kz
     for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
       const int l = e / n, kz = e - l * n;
-      const int kx = a0 + l;
-      const int ky = (int)b;
-      const double tx = sp.tr[0][kx], ty = sp.tr[1][ky], tz = sp.tr[2][kz];
-      const double pyz = __dmul_rn(ty, tz), pxz = __dmul_rn(tx, tz), pxy = __dmul_rn(tx, ty);
-      const double kk = __dadd_rn(__dadd_rn(__dmul_rn(sp.k2[0][kx], __dmul_rn(pyz, pyz)),
-                                            __dmul_rn(sp.k2[1][ky], __dmul_rn(pxz, pxz))),
-                                  __dmul_rn(sp.k2[2][kz], __dmul_rn(pxy, pxy)));
-      C v = buf[l * lstride + kz];
-      if (kk < 1.0e-16) {
-        v = C{(R)0, (R)0};
-      } else {
-        const double f = -sp.scale / kk;
-        v = C{(R)(v.x * f), (R)(v.y * f)};
-      }
-      buf[l * lstride + kz] = v;
+      buf[l * lstride + kz] = Spectral<P>::apply(buf[l * lstride + kz], sp, a0 + l, (int)b, kz);
     }
     __syncthreads();
-    smem_fft<1>(buf, lstride, n, nl, tw_i);
+    smem_fft<1, P>(buf, lstride, n, nl, tw_i);
   }
   for (int e = threadIdx.x; e < lanes * n; e += FFT_THREADS) {
     const int r = e / lanes, l = e - r * lanes;
@@ -263,12 +396,6 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_strided(typename Cx<R>::T* __
 }
 
 bool pow2(int n) { return n >= 2 && (n & (n - 1)) == 0; }
-
-template <typename R>
-struct FftTables {
-  // per axis: twiddles for the complex FFT length (forward/inverse), plus
-  // full-length twiddles for the x split.
-};
 
 }  // namespace
 
@@ -305,21 +432,38 @@ static int fft_setup(Ctx* c) {
   twiddles(ny, +1, t);
   twiddles(nz, -1, t);
   twiddles(nz, +1, t);
-  std::vector<float> t32(t.size());
-  for (size_t i = 0; i < t.size(); ++i) t32[i] = (float)t[i];
+  std::vector<float> t32(t.size()), tdf(2 * t.size());
+  for (size_t i = 0; i < t.size(); ++i) {
+    t32[i] = (float)t[i];
+    tdf[2 * i] = (float)t[i];
+    tdf[2 * i + 1] = (float)(t[i] - (double)tdf[2 * i]);
+  }
   if (cudaMalloc(&c->d_twid, t.size() * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
   if (cudaMalloc(&c->d_twid32, t32.size() * sizeof(float)) != cudaSuccess) return X3D_ERR_NOMEM;
+  if (cudaMalloc(&c->d_twid_df, tdf.size() * sizeof(float)) != cudaSuccess) return X3D_ERR_NOMEM;
   cudaMemcpy(c->d_twid, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_twid32, t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemcpy(c->d_twid_df, tdf.data(), tdf.size() * sizeof(float), cudaMemcpyHostToDevice);
   c->twid_n = (int)t.size() / 2;
-  // Poisson tables
+  // Poisson tables (binary64 and hi/lo binary32 pairs)
   for (int ax = 0; ax < 3; ++ax) {
     dvec k2, tr;
     waves_tables(c->ax[ax], k2, tr);
+    std::vector<float> k2s(2 * k2.size()), trs(2 * tr.size());
+    for (size_t i = 0; i < k2.size(); ++i) {
+      k2s[2 * i] = (float)k2[i];
+      k2s[2 * i + 1] = (float)(k2[i] - (double)k2s[2 * i]);
+      trs[2 * i] = (float)tr[i];
+      trs[2 * i + 1] = (float)(tr[i] - (double)trs[2 * i]);
+    }
     if (cudaMalloc(&c->d_k2[ax], k2.size() * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
     if (cudaMalloc(&c->d_tr[ax], tr.size() * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
+    if (cudaMalloc(&c->d_k2df[ax], k2s.size() * sizeof(float)) != cudaSuccess) return X3D_ERR_NOMEM;
+    if (cudaMalloc(&c->d_trdf[ax], trs.size() * sizeof(float)) != cudaSuccess) return X3D_ERR_NOMEM;
     cudaMemcpy(c->d_k2[ax], k2.data(), k2.size() * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(c->d_tr[ax], tr.data(), tr.size() * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(c->d_k2df[ax], k2s.data(), k2s.size() * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemcpy(c->d_trdf[ax], trs.data(), trs.size() * sizeof(float), cudaMemcpyHostToDevice);
   }
   return cuda_status(cudaGetLastError());
 }
@@ -338,7 +482,10 @@ static int poisson_run(Ctx* c, double* rhs, cudaStream_t st) {
     c->fft_work_bytes = need;
   }
   C* spec = reinterpret_cast<C*>(c->fft_work);
-  const C* tw = reinterpret_cast<const C*>(sizeof(R) == 8 ? (const void*)c->d_twid : (const void*)c->d_twid32);
+  const void* twv = std::is_same<R, double>::value ? (const void*)c->d_twid
+                    : std::is_same<R, float>::value ? (const void*)c->d_twid32
+                                                    : (const void*)c->d_twid_df;
+  const C* tw = reinterpret_cast<const C*>(twv);
   const C* twx_f = tw;
   const C* twx_i = tw + M;
   const C* twx_full = tw + 2 * M;
@@ -348,7 +495,12 @@ static int poisson_run(Ctx* c, double* rhs, cudaStream_t st) {
   const C* twz_i = twz_f + nz;
 
   Spec sp;
-  for (int a = 0; a < 3; ++a) { sp.k2[a] = c->d_k2[a]; sp.tr[a] = c->d_tr[a]; }
+  for (int a = 0; a < 3; ++a) {
+    sp.k2[a] = c->d_k2[a];
+    sp.tr[a] = c->d_tr[a];
+    sp.k2df[a] = c->d_k2df[a];
+    sp.trdf[a] = c->d_trdf[a];
+  }
   sp.nx = nx; sp.ny = ny; sp.nz = nz;
   sp.scale = 1.0 / ((double)nx * (double)ny * (double)nz);
 
@@ -410,6 +562,7 @@ int poisson_periodic(Ctx* c, double* rhs, int precision, cudaStream_t st) {
   if (rc != X3D_OK) return rc;
   if (precision == 0) return poisson_run<double>(c, rhs, st);
   if (precision == 1) return poisson_run<float>(c, rhs, st);
+  if (precision == 2) return poisson_run<DF>(c, rhs, st);
   return X3D_ERR_DTYPE;
 }
 
@@ -554,6 +707,7 @@ int poisson_periodic_noalloc(Ctx* c, double* rhs, cudaStream_t st) {
   const C* twz_f = twy_i + ny;
   const C* twz_i = twz_f + nz;
   Spec sp;
+  std::memset(&sp, 0, sizeof(sp));
   sp.k2[0] = k2; sp.k2[1] = k2 + nx; sp.k2[2] = k2 + nx + ny;
   sp.tr[0] = tr; sp.tr[1] = tr + nx; sp.tr[2] = tr + nx + ny;
   sp.nx = nx; sp.ny = ny; sp.nz = nz;

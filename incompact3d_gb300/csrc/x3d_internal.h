@@ -108,6 +108,9 @@ struct Ctx {
   double* d_tr[3] = {nullptr, nullptr, nullptr};
   double* d_twid = nullptr;  // FFT twiddles (see x3d_fft.cu)
   float* d_twid32 = nullptr;
+  float* d_twid_df = nullptr;             // twiddles as binary32 hi/lo pairs
+  float2* d_k2df[3] = {nullptr, nullptr, nullptr};  // k2 / transfer tables as hi/lo pairs
+  float2* d_trdf[3] = {nullptr, nullptr, nullptr};
   int twid_n = 0;
   void* fft_work = nullptr;  // complex spectrum buffer
   size_t fft_work_bytes = 0;

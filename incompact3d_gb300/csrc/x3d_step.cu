@@ -79,19 +79,38 @@ __global__ void k_final3(H* o1, H* o2, H* o3, const T* a1, const T* a2, const T*
   }
 }
 
-// Adams-Bashforth / RK update of one component, in FP64:
-//   u = c1*h1 + c2*h2 + c3*h3 + u   (terms with a null pointer are skipped)
-// and, when u32 is non-null, an FP32 copy of the new u for the next operators.
-template <typename H>
-__global__ void k_intt(double* u, float* u32, const H* h1, const H* h2, const H* h3, double c1, double c2, double c3,
-                       long long n) {
+// Adams-Bashforth / RK update, FP64 operators:
+//   u = c1*h1 + c2*h2 + c3*h3 + u   (nh = number of history terms used)
+__global__ void k_intt64(double* u, const double* h1, const double* h2, const double* h3, double c1, double c2,
+                         double c3, int nh, long long n) {
   GRID_STRIDE(i, n) {
-    double acc = c1 * (double)h1[i];
-    if (h2) acc = acc + c2 * (double)h2[i];
-    if (h3) acc = acc + c3 * (double)h3[i];
-    const double v = acc + u[i];
-    u[i] = v;
-    if (u32) u32[i] = (float)v;
+    double acc = c1 * h1[i];
+    if (nh > 1) acc = acc + c2 * h2[i];
+    if (nh > 2) acc = acc + c3 * h3[i];
+    u[i] = acc + u[i];
+  }
+}
+
+// Mixed precision: the increment sum(c_k h_k) of the FP32 right-hand sides is
+// formed in FP32 (it carries the FP32 accuracy of the h_k anyway) and added to
+// the FP64 state in FP64; the FP32 operator copy of u is refreshed.  The three
+// velocity components are updated in one launch.
+struct Intt3 {
+  double* u[3];
+  float* u32[3];
+  const float* h[3][3];
+};
+__global__ void k_intt_mixed(Intt3 a, float c1, float c2, float c3, int nh, long long n) {
+  GRID_STRIDE(i, n) {
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      float inc = c1 * a.h[q][0][i];
+      if (nh > 1) inc = inc + c2 * a.h[q][1][i];
+      if (nh > 2) inc = inc + c3 * a.h[q][2][i];
+      const double v = (double)inc + a.u[q][i];
+      a.u[q][i] = v;
+      a.u32[q][i] = (float)v;
+    }
   }
 }
 
@@ -109,16 +128,29 @@ __global__ void k_to32(float* o, const double* a, long long n) {
   GRID_STRIDE(i, n) o[i] = (float)a[i];
 }
 
-// u -= px (cor_vel), FP64 state, optional FP32 copy
+// u -= px (cor_vel), FP64 state
 template <typename T>
-__global__ void k_corvel(double* u1, double* u2, double* u3, float* v1, float* v2, float* v3, const T* p1,
-                         const T* p2, const T* p3, long long n) {
+__global__ void k_corvel(double* u1, double* u2, double* u3, const T* p1, const T* p2, const T* p3, long long n) {
   GRID_STRIDE(i, n) {
-    const double a = u1[i] - (double)p1[i];
-    const double b = u2[i] - (double)p2[i];
-    const double c = u3[i] - (double)p3[i];
-    u1[i] = a; u2[i] = b; u3[i] = c;
-    if (v1) { v1[i] = (float)a; v2[i] = (float)b; v3[i] = (float)c; }
+    u1[i] = u1[i] - (double)p1[i];
+    u2[i] = u2[i] - (double)p2[i];
+    u3[i] = u3[i] - (double)p3[i];
+  }
+}
+
+// Mixed precision cor_vel: FP64 state minus the FP32 gradient; the FP32
+// operator copy is updated by the same subtraction in FP32 (within one ulp of
+// rounding the new FP64 state), which saves the FP64->FP32 conversions.
+__global__ void k_corvel_mixed(double* u1, double* u2, double* u3, float* v1, float* v2, float* v3, const float* p1,
+                               const float* p2, const float* p3, long long n) {
+  GRID_STRIDE(i, n) {
+    const float a = p1[i], b = p2[i], c = p3[i];
+    u1[i] = u1[i] - (double)a;
+    u2[i] = u2[i] - (double)b;
+    u3[i] = u3[i] - (double)c;
+    v1[i] = v1[i] - a;
+    v2[i] = v2[i] - b;
+    v3[i] = v3[i] - c;
   }
 }
 
@@ -379,21 +411,33 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
   const int it = s->itime + 1;
   double* U[3] = {s->ux, s->uy, s->uz};
   float* U32[3] = {s->ux32, s->uy32, s->uz32};
-  for (int q = 0; q < 3; ++q) {
-    const T* h1 = (const T*)s->H[q][0];
-    const T* h2 = (const T*)s->H[q][1];
-    const T* h3 = (const T*)s->H[q][2];
-    float* o32 = mixed ? U32[q] : nullptr;
-    const double dt = s->o.dt;
-    if (s->o.itimescheme == 3) {
-      if (it == 1) k_intt<T><<<nb, 256, 0, st>>>(U[q], o32, h1, nullptr, nullptr, dt, 0, 0, N);
-      else if (it == 2) k_intt<T><<<nb, 256, 0, st>>>(U[q], o32, h1, h2, nullptr, 1.5 * dt, -0.5 * dt, 0, N);
-      else k_intt<T><<<nb, 256, 0, st>>>(U[q], o32, h1, h2, h3, s->adt[0], s->bdt[0], s->cdt[0], N);
-    } else {
-      if (itr == 1) k_intt<T><<<nb, 256, 0, st>>>(U[q], o32, h1, nullptr, nullptr, s->gdt[0], 0, 0, N);
-      else k_intt<T><<<nb, 256, 0, st>>>(U[q], o32, h1, h2, nullptr, s->adt[itr - 1], s->bdt[itr - 1], 0, N);
+  // coefficients and number of history terms of this sub-step
+  const double dt = s->o.dt;
+  double c1 = 0, c2 = 0, c3 = 0;
+  int nh = 1;
+  if (s->o.itimescheme == 3) {
+    if (it == 1) { c1 = dt; nh = 1; }
+    else if (it == 2) { c1 = 1.5 * dt; c2 = -0.5 * dt; nh = 2; }
+    else { c1 = s->adt[0]; c2 = s->bdt[0]; c3 = s->cdt[0]; nh = 3; }
+  } else {
+    if (itr == 1) { c1 = s->gdt[0]; nh = 1; }
+    else { c1 = s->adt[itr - 1]; c2 = s->bdt[itr - 1]; nh = 2; }
+  }
+  if (mixed) {
+    Intt3 a;
+    for (int q = 0; q < 3; ++q) {
+      a.u[q] = U[q];
+      a.u32[q] = U32[q];
+      for (int k = 0; k < 3; ++k) a.h[q][k] = (const float*)s->H[q][k];
     }
+    k_intt_mixed<<<nb, 256, 0, st>>>(a, (float)c1, (float)c2, (float)c3, nh, N);
     s->launches++;
+  } else {
+    for (int q = 0; q < 3; ++q) {
+      k_intt64<<<nb, 256, 0, st>>>(U[q], (const double*)s->H[q][0], (const double*)s->H[q][1],
+                                   (const double*)s->H[q][2], c1, c2, c3, nh, N);
+      s->launches++;
+    }
   }
   // history rotation: dvar(3)=dvar(2); dvar(2)=dvar(1)
   for (int q = 0; q < 3; ++q) {
@@ -414,7 +458,8 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
   const T* vy = mixed ? (const T*)s->uy32 : (const T*)s->uy;
   const T* vz = mixed ? (const T*)s->uz32 : (const T*)s->uz;
   RC(divergence<T>(s, vx, vy, vz, s->pp64, st));
-  RC(poisson_periodic(c, s->pp64, 0, st));
+  // mixed: FP64-class Poisson solve in double-float arithmetic on the FP32 pipes
+  RC(poisson_periodic(c, s->pp64, mixed ? 2 : 0, st));
   s->launches += 5;
   const T* pin = (const T*)s->pp64;
   T** w = reinterpret_cast<T**>(s->W);
@@ -424,8 +469,11 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
     pin = (const T*)w[12];
   }
   RC(gradp<T>(s, pin, w[0], w[1], w[2], st));
-  k_corvel<T><<<nb, 256, 0, st>>>(s->ux, s->uy, s->uz, mixed ? s->ux32 : nullptr, mixed ? s->uy32 : nullptr,
-                                  mixed ? s->uz32 : nullptr, w[0], w[1], w[2], N);
+  if (mixed)
+    k_corvel_mixed<<<nb, 256, 0, st>>>(s->ux, s->uy, s->uz, s->ux32, s->uy32, s->uz32, (const float*)w[0],
+                                       (const float*)w[1], (const float*)w[2], N);
+  else
+    k_corvel<T><<<nb, 256, 0, st>>>(s->ux, s->uy, s->uz, w[0], w[1], w[2], N);
   s->launches++;
   return cuda_status(cudaGetLastError());
 }
@@ -691,8 +739,7 @@ int x3d_cor_vel(x3d_ctx* h, double* ux, double* uy, double* uz, const double* px
   if (!h || !ux || !uy || !uz || !px || !py || !pz) return X3D_ERR_ARG;
   Ctx* c = reinterpret_cast<Ctx*>(h);
   const long long N = (long long)c->grid.nx * c->grid.ny * c->grid.nz;
-  k_corvel<double><<<pw_blocks(c, N), 256, 0, (cudaStream_t)stream>>>(ux, uy, uz, nullptr, nullptr, nullptr, px, py,
-                                                                      pz, N);
+  k_corvel<double><<<pw_blocks(c, N), 256, 0, (cudaStream_t)stream>>>(ux, uy, uz, px, py, pz, N);
   return cuda_status(cudaGetLastError());
 }
 

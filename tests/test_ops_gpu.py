@@ -157,4 +157,6 @@ def test_fp32_fast_path_periodic(oracle_mod, gpu_lib, n):
         for kind in range(7):
             ref = o.op(axis, kind, 1, u)
             got = ctx.apply(axis, kind, 1, ud).double().cpu().numpy()
-            assert relerr(got, ref) < 1e-4, (n, axis, OPS[kind], relerr(got, ref))
+            # binary32 round-off of the second difference grows like (n/(2 pi k))^2
+            tol = 1e-4 * max(1.0, (n / 256.0) ** 2) if kind == 1 else 1e-4
+            assert relerr(got, ref) < tol, (n, axis, OPS[kind], relerr(got, ref))

@@ -10,8 +10,10 @@ pytestmark = pytest.mark.gpu
 L = 2 * np.pi
 
 
-@pytest.mark.parametrize("dims", [(16, 16, 16), (32, 32, 32), (64, 16, 32), (16, 64, 8)])
-def test_poisson_matches_oracle(oracle_mod, gpu_lib, dims):
+@pytest.mark.parametrize("precision", [0, 2], ids=["fp64", "double_float"])
+@pytest.mark.parametrize("dims", [(16, 16, 16), (32, 32, 32), (64, 16, 32), (16, 64, 8), (128, 64, 32)])
+def test_poisson_matches_oracle(oracle_mod, gpu_lib, dims, precision):
+    """FP64 FFT and double-float FFT (binary32 hi/lo pairs) vs the oracle."""
     import torch
     ctx = gpu_lib.Context(*dims, L, 2.0, 3.0)
     o = oracle_mod.Oracle(*dims, L, 2.0, 3.0)
@@ -20,9 +22,9 @@ def test_poisson_matches_oracle(oracle_mod, gpu_lib, dims):
     rhs -= rhs.mean()
     ref = o.poisson(rhs)
     d = torch.from_numpy(rhs).cuda()
-    ctx.poisson(d)
+    ctx.poisson(d, precision=precision)
     got = d.cpu().numpy()
-    assert relerr(got, ref) < 1e-12
+    assert relerr(got, ref) < 1e-12, relerr(got, ref)
 
 
 def test_poisson_fp32_fft_close(oracle_mod, gpu_lib):
