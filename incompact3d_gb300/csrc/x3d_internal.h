@@ -124,9 +124,25 @@ int ctx_workspace(Ctx* c, size_t bytes, void** out);
 // Get (building on first use) the device plan of an operator.
 int get_plan(Ctx* c, int axis, int kind, int npaire, int coefset, OpPlan** out);
 
-// Launch the generic line kernel.  T = double or float.
+// Optional fusion of the pointwise work around a compact operator:
+//   input  u = in * in2                       (in2 != null)
+//   output o = cr*t + c1*a1 + c2*a2 + y*t     (active != 0; null operands skipped)
+// a1, a2, y have the output's layout; the output may alias a1 or a2.
 template <typename T>
-int launch_line_op(Ctx* c, OpPlan* p, T* out, const T* in, const int* dims_in, const T* pp, cudaStream_t st);
+struct Fuse {
+  const T* in2 = nullptr;
+  const T* a1 = nullptr;
+  const T* a2 = nullptr;
+  const T* y = nullptr;
+  T cr = T(1), c1 = T(0), c2 = T(0);
+  int active = 0;
+};
+
+// Launch the compact-operator line kernel (generic or fast path).  T = double
+// or float; fz may be null.
+template <typename T>
+int launch_line_op(Ctx* c, OpPlan* p, T* out, const T* in, const int* dims_in, const T* pp, cudaStream_t st,
+                   const Fuse<T>* fz = nullptr);
 
 // Host copy of a plan: sc[16] scalars, vecs[6*nout] = s,f,w,pf,qb,rsm,
 // brows[kMaxBRows*(2+kMaxTerms*(2+2*kMaxEnt))].  Returns nout or an error.

@@ -34,6 +34,7 @@ struct FastArgs {
   T qbs[FCHUNKS];                // qb at each chunk's first row
   int mode[FCHUNKS];             // bit0: uniform factors, bit1: SM vector non-zero
   int nterms_int;
+  Fuse<T> fz;                    // optional product on load / combination on store
 };
 
 template <int KIND>
@@ -92,18 +93,36 @@ __global__ void __launch_bounds__(LANES* FCHUNKS) line_fast(const __grid_constan
   T w[WN];
   if (!XL) {
     const bool ok = lane < nl;
-    const T* src = p.in + (ok ? (long long)(a0 + lane) * p.sa : 0) + b * p.sb;
+    const long long off = (ok ? (long long)(a0 + lane) * p.sa : 0) + b * p.sb;
+    const T* src = p.in + off;
+    if (p.fz.in2) {
+      const T* src2 = p.fz.in2 + off;
 #pragma unroll
-    for (int j = 0; j < WN; ++j) {
-      int r = r0 - LO + j;
-      r = (r < 0) ? r + n : (r >= n ? r - n : r);
-      w[j] = ok ? src[(long long)r * p.rs] : T(0);
+      for (int j = 0; j < WN; ++j) {
+        int r = r0 - LO + j;
+        r = (r < 0) ? r + n : (r >= n ? r - n : r);
+        w[j] = ok ? src[(long long)r * p.rs] * src2[(long long)r * p.rs] : T(0);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < WN; ++j) {
+        int r = r0 - LO + j;
+        r = (r < 0) ? r + n : (r >= n ? r - n : r);
+        w[j] = ok ? src[(long long)r * p.rs] : T(0);
+      }
     }
   } else {
-    const T* src = p.in + (long long)a0 * p.sa + b * p.sb;
+    const long long off = (long long)a0 * p.sa + b * p.sb;
+    const T* src = p.in + off;
+    const T* src2 = p.fz.in2 ? p.fz.in2 + off : nullptr;
     for (int l = ch; l < LANES; l += FCHUNKS) {
       if (l < nl) {
-        for (int r = lane; r < n; r += LANES) tile[r * LD + l] = src[(long long)l * p.sa + r];
+        if (src2) {
+          for (int r = lane; r < n; r += LANES)
+            tile[r * LD + l] = src[(long long)l * p.sa + r] * src2[(long long)l * p.sa + r];
+        } else {
+          for (int r = lane; r < n; r += LANES) tile[r * LD + l] = src[(long long)l * p.sa + r];
+        }
       } else {
         for (int r = lane; r < n; r += LANES) tile[r * LD + l] = T(0);
       }
@@ -181,21 +200,39 @@ __global__ void __launch_bounds__(LANES* FCHUNKS) line_fast(const __grid_constan
     for (int k = 0; k < L; ++k) v[k] = v[k] - sx * p.rsm[r0 + k];
   }
 
-  // 6. store
+  // 6. store (with the optional combination epilogue)
   if (!XL) {
     if (lane < nl) {
-      T* dst = p.out + (long long)(a0 + lane) * p.sa + b * p.sb;
+      const long long off = (long long)(a0 + lane) * p.sa + b * p.sb;
+      T* dst = p.out + off;
+      if (p.fz.active) {
 #pragma unroll
-      for (int k = 0; k < L; ++k) dst[(long long)(r0 + k) * p.rs] = v[k];
+        for (int k = 0; k < L; ++k) {
+          const long long i = (long long)(r0 + k) * p.rs;
+          dst[i] = fuse_out(p.fz, v[k], off + i);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < L; ++k) dst[(long long)(r0 + k) * p.rs] = v[k];
+      }
     }
   } else {
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < L; ++k) tile[(r0 + k) * LD + lane] = v[k];
     __syncthreads();
-    T* dst = p.out + (long long)a0 * p.sa + b * p.sb;
-    for (int l = ch; l < nl; l += FCHUNKS)
-      for (int r = lane; r < n; r += LANES) dst[(long long)l * p.sa + r] = tile[r * LD + l];
+    const long long off = (long long)a0 * p.sa + b * p.sb;
+    T* dst = p.out + off;
+    if (p.fz.active) {
+      for (int l = ch; l < nl; l += FCHUNKS)
+        for (int r = lane; r < n; r += LANES) {
+          const long long i = (long long)l * p.sa + r;
+          dst[i] = fuse_out(p.fz, tile[r * LD + l], off + i);
+        }
+    } else {
+      for (int l = ch; l < nl; l += FCHUNKS)
+        for (int r = lane; r < n; r += LANES) dst[(long long)l * p.sa + r] = tile[r * LD + l];
+    }
   }
 }
 

@@ -44,6 +44,15 @@ struct BRowD {
 };
 
 template <typename T>
+__device__ __forceinline__ T fuse_out(const Fuse<T>& f, T t, long long i) {
+  T o = (f.cr != T(0)) ? f.cr * t : T(0);
+  if (f.a1) o = o + f.c1 * f.a1[i];
+  if (f.a2) o = o + f.c2 * f.a2[i];
+  if (f.y) o = o + f.y[i] * t;
+  return o;
+}
+
+template <typename T>
 struct LineArgs {
   const T* in;
   T* out;
@@ -53,6 +62,7 @@ struct LineArgs {
   T ca, cb, cc, cd, alpha, den;
   int periodic, nterms_int, nbrows;
   BRowD<T> brows[kMaxBRows];
+  Fuse<T> fz;
 };
 
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
@@ -147,13 +157,21 @@ __global__ void __launch_bounds__(LANES* CHUNKS) line_kernel(const __grid_consta
   if (!XL) {
     const int a = a0 + lane;
     const bool ok = lane < nl;
-    const T* src = p.in + (ok ? (long long)a * p.sa_in : 0) + b * p.sb_in;
-    for (int r = ch; r < nin; r += CHUNKS) tile[r * LD + lane] = ok ? src[r * p.rs_in] : T(0);
+    const long long off = (ok ? (long long)a * p.sa_in : 0) + b * p.sb_in;
+    const T* src = p.in + off;
+    const T* src2 = p.fz.in2 ? p.fz.in2 + off : nullptr;
+    for (int r = ch; r < nin; r += CHUNKS)
+      tile[r * LD + lane] = ok ? (src2 ? src[r * p.rs_in] * src2[r * p.rs_in] : src[r * p.rs_in]) : T(0);
   } else {
-    const T* src = p.in + (long long)a0 * p.sa_in + b * p.sb_in;
+    const long long off = (long long)a0 * p.sa_in + b * p.sb_in;
+    const T* src = p.in + off;
+    const T* src2 = p.fz.in2 ? p.fz.in2 + off : nullptr;
     for (int l = ch; l < LANES; l += CHUNKS) {
       if (l < nl) {
-        for (int r = lane; r < nin; r += LANES) tile[r * LD + l] = src[(long long)l * p.sa_in + r];
+        for (int r = lane; r < nin; r += LANES) {
+          const long long i = (long long)l * p.sa_in + r;
+          tile[r * LD + l] = src2 ? src[i] * src2[i] : src[i];
+        }
       } else {
         for (int r = lane; r < nin; r += LANES) tile[r * LD + l] = T(0);
       }
@@ -246,14 +264,15 @@ __global__ void __launch_bounds__(LANES* CHUNKS) line_kernel(const __grid_consta
     }
   }
 
-  // 6. store
+  // 6. store (with the optional combination epilogue)
   if (!XL) {
     if (lane < nl) {
-      T* dst = p.out + (long long)(a0 + lane) * p.sa_out + b * p.sb_out;
+      const long long off = (long long)(a0 + lane) * p.sa_out + b * p.sb_out;
+      T* dst = p.out + off;
 #pragma unroll
       for (int k = 0; k < LMAX; ++k) {
         const int r = r0 + k;
-        if (r < r1) dst[r * p.rs_out] = v[k];
+        if (r < r1) dst[r * p.rs_out] = p.fz.active ? fuse_out(p.fz, v[k], off + r * p.rs_out) : v[k];
       }
     }
   } else {
@@ -264,9 +283,13 @@ __global__ void __launch_bounds__(LANES* CHUNKS) line_kernel(const __grid_consta
       if (r < r1) tile[r * LD + lane] = v[k];
     }
     __syncthreads();
-    T* dst = p.out + (long long)a0 * p.sa_out + b * p.sb_out;
+    const long long off = (long long)a0 * p.sa_out + b * p.sb_out;
+    T* dst = p.out + off;
     for (int l = ch; l < nl; l += CHUNKS)
-      for (int r = lane; r < nout; r += LANES) dst[(long long)l * p.sa_out + r] = tile[r * LD + l];
+      for (int r = lane; r < nout; r += LANES) {
+        const long long i = (long long)l * p.sa_out + r;
+        dst[i] = p.fz.active ? fuse_out(p.fz, tile[r * LD + l], off + i) : tile[r * LD + l];
+      }
   }
 }
 

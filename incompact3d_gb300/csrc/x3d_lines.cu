@@ -39,7 +39,8 @@ int fdispatch(const FastArgs<float>& a, int kind, bool xl, int L, dim3 grid, siz
 }
 
 // Periodic lines of 16*L points (L = 8, 16, 32) in FP32 take the fast path.
-int launch_fast(OpPlan* p, float* out, const float* in, const int* dims_in, cudaStream_t st) {
+int launch_fast(OpPlan* p, float* out, const float* in, const int* dims_in, cudaStream_t st,
+                const Fuse<float>* fz) {
   const int n = p->nout;
   const int L = n / FCHUNKS;
   FastArgs<float> a;
@@ -85,6 +86,7 @@ int launch_fast(OpPlan* p, float* out, const float* in, const int* dims_in, cuda
     }
     a.mode[c] = (uni ? 1 : 0) | (sm ? 2 : 0);
   }
+  if (fz) a.fz = *fz;
   const size_t smem = fast_smem<float>(n, xl);
   return fdispatch(a, p->kind, xl, L, grid, smem, st);
 }
@@ -154,14 +156,15 @@ static int upload_plan(OpPlan* p) {
 }
 
 template <typename T>
-int launch_line_op(Ctx* c, OpPlan* p, T* out, const T* in, const int* dims_in, const T* pp, cudaStream_t st) {
+int launch_line_op(Ctx* c, OpPlan* p, T* out, const T* in, const int* dims_in, const T* pp, cudaStream_t st,
+                   const Fuse<T>* fz) {
   if (!out || !in) return X3D_ERR_ARG;
   if (dims_in[p->axis] != p->nin) return X3D_ERR_SHAPE;
   const int up = upload_plan(p);
   if (up != X3D_OK) return up;
   if (std::is_same<T, float>::value && p->periodic && p->nin == p->nout && pp == nullptr && c->fast_lines &&
       p->nout % FCHUNKS == 0 && (p->nout / FCHUNKS == 8 || p->nout / FCHUNKS == 16 || p->nout / FCHUNKS == 32))
-    return launch_fast(p, (float*)out, (const float*)in, dims_in, st);
+    return launch_fast(p, (float*)out, (const float*)in, dims_in, st, (const Fuse<float>*)fz);
   LineArgs<T> a;
   std::memset(&a, 0, sizeof(a));
   a.in = in;
@@ -215,6 +218,7 @@ int launch_line_op(Ctx* c, OpPlan* p, T* out, const T* in, const int* dims_in, c
       }
     }
   }
+  if (fz) a.fz = *fz;
   const int lmax = (p->L <= 8) ? 8 : 32;
   const size_t smem = line_smem<T>(p->nin, p->nout);
   if (smem > 227 * 1024) return X3D_ERR_UNSUPPORTED;
@@ -255,7 +259,9 @@ int plan_info(Ctx* c, int axis, int kind, int npaire, int coefset, double* sc, d
   return n;
 }
 
-template int launch_line_op<double>(Ctx*, OpPlan*, double*, const double*, const int*, const double*, cudaStream_t);
-template int launch_line_op<float>(Ctx*, OpPlan*, float*, const float*, const int*, const float*, cudaStream_t);
+template int launch_line_op<double>(Ctx*, OpPlan*, double*, const double*, const int*, const double*, cudaStream_t,
+                                   const Fuse<double>*);
+template int launch_line_op<float>(Ctx*, OpPlan*, float*, const float*, const int*, const float*, cudaStream_t,
+                                  const Fuse<float>*);
 
 }  // namespace x3d

@@ -33,52 +33,6 @@ inline unsigned pw_blocks(Ctx* c, long long n) {
 #define GRID_STRIDE(i, n) \
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (n); i += (long long)gridDim.x * blockDim.x)
 
-// o_k = x_k * y
-template <typename T>
-__global__ void k_prod3(T* o1, T* o2, T* o3, const T* x1, const T* x2, const T* x3, const T* y, long long n) {
-  GRID_STRIDE(i, n) {
-    const T yy = y[i];
-    o1[i] = x1[i] * yy;
-    o2[i] = x2[i] * yy;
-    o3[i] = x3[i] * yy;
-  }
-}
-
-// o_k = a_k + y * b_k
-template <typename T>
-__global__ void k_addmul3(T* o1, T* o2, T* o3, const T* a1, const T* a2, const T* a3, const T* b1, const T* b2,
-                          const T* b3, const T* y, long long n) {
-  GRID_STRIDE(i, n) {
-    const T yy = y[i];
-    o1[i] = a1[i] + yy * b1[i];
-    o2[i] = a2[i] + yy * b2[i];
-    o3[i] = a3[i] + yy * b3[i];
-  }
-}
-
-// o_k = s1 * a_k + s2 * b_k
-template <typename T>
-__global__ void k_lin3(T* o1, T* o2, T* o3, const T* a1, const T* a2, const T* a3, const T* b1, const T* b2,
-                       const T* b3, T s1, T s2, long long n) {
-  GRID_STRIDE(i, n) {
-    o1[i] = s1 * a1[i] + s2 * b1[i];
-    o2[i] = s1 * a2[i] + s2 * b2[i];
-    o3[i] = s1 * a3[i] + s2 * b3[i];
-  }
-}
-
-// H_k = a_k - 0.5 * b_k + xnu * c_k  (final sum of momentum_rhs_eq; output may
-// be a different precision than the operands)
-template <typename T, typename H>
-__global__ void k_final3(H* o1, H* o2, H* o3, const T* a1, const T* a2, const T* a3, const T* b1, const T* b2,
-                         const T* b3, const T* c1, const T* c2, const T* c3, T xnu, long long n) {
-  GRID_STRIDE(i, n) {
-    o1[i] = (H)(a1[i] - T(0.5) * b1[i] + xnu * c1[i]);
-    o2[i] = (H)(a2[i] - T(0.5) * b2[i] + xnu * c2[i]);
-    o3[i] = (H)(a3[i] - T(0.5) * b3[i] + xnu * c3[i]);
-  }
-}
-
 // Adams-Bashforth / RK update, FP64 operators:
 //   u = c1*h1 + c2*h2 + c3*h3 + u   (nh = number of history terms used)
 __global__ void k_intt64(double* u, const double* h1, const double* h2, const double* h3, double c1, double c2,
@@ -91,27 +45,71 @@ __global__ void k_intt64(double* u, const double* h1, const double* h2, const do
   }
 }
 
-// Mixed precision: the increment sum(c_k h_k) of the FP32 right-hand sides is
-// formed in FP32 (it carries the FP32 accuracy of the h_k anyway) and added to
-// the FP64 state in FP64; the FP32 operator copy of u is refreshed.  The three
-// velocity components are updated in one launch.
+// Mixed precision keeps the velocity as a double-float pair (hi, lo) of
+// binary32 arrays: hi is exactly the FP32 operand the operators read, and the
+// pair carries ~48 significand bits, so the state is accumulated to FP64-class
+// accuracy with FP32 instructions only (GB300's FP64 pipe is 1/64 of FP32).
+__device__ __forceinline__ void df_add_f(float& h, float& l, float b) {
+  const float s = __fadd_rn(h, b);
+  const float v = __fsub_rn(s, h);
+  float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, v)), __fsub_rn(b, v));
+  e = __fadd_rn(e, l);
+  const float hh = __fadd_rn(s, e);
+  l = __fsub_rn(e, __fsub_rn(hh, s));
+  h = hh;
+}
+
+// AB/RK update of the double-float state: (h,l) += sum(c_k h_k), the increment
+// formed in FP32 (it carries the FP32 accuracy of the right-hand sides).
 struct Intt3 {
-  double* u[3];
-  float* u32[3];
+  float* uh[3];
+  float* ul[3];
   const float* h[3][3];
 };
-__global__ void k_intt_mixed(Intt3 a, float c1, float c2, float c3, int nh, long long n) {
+__global__ void k_intt_df(Intt3 a, float c1, float c2, float c3, int nh, long long n) {
   GRID_STRIDE(i, n) {
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
       float inc = c1 * a.h[q][0][i];
       if (nh > 1) inc = inc + c2 * a.h[q][1][i];
       if (nh > 2) inc = inc + c3 * a.h[q][2][i];
-      const double v = (double)inc + a.u[q][i];
-      a.u[q][i] = v;
-      a.u32[q][i] = (float)v;
+      float h = a.uh[q][i], l = a.ul[q][i];
+      df_add_f(h, l, inc);
+      a.uh[q][i] = h;
+      a.ul[q][i] = l;
     }
   }
+}
+
+// cor_vel on the double-float state: u -= grad p (FP32 gradient)
+struct Cor3 {
+  float* uh[3];
+  float* ul[3];
+  const float* p[3];
+};
+__global__ void k_corvel_df(Cor3 a, long long n) {
+  GRID_STRIDE(i, n) {
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      float h = a.uh[q][i], l = a.ul[q][i];
+      df_add_f(h, l, -a.p[q][i]);
+      a.uh[q][i] = h;
+      a.ul[q][i] = l;
+    }
+  }
+}
+
+__global__ void k_split(float* h, float* l, const double* d, long long n) {
+  GRID_STRIDE(i, n) {
+    const double v = d[i];
+    const float hi = (float)v;
+    h[i] = hi;
+    l[i] = (float)(v - (double)hi);
+  }
+}
+
+__global__ void k_combine(double* d, const float* h, const float* l, long long n) {
+  GRID_STRIDE(i, n) d[i] = (double)h[i] + (double)l[i];
 }
 
 template <typename T>
@@ -135,22 +133,6 @@ __global__ void k_corvel(double* u1, double* u2, double* u3, const T* p1, const 
     u1[i] = u1[i] - (double)p1[i];
     u2[i] = u2[i] - (double)p2[i];
     u3[i] = u3[i] - (double)p3[i];
-  }
-}
-
-// Mixed precision cor_vel: FP64 state minus the FP32 gradient; the FP32
-// operator copy is updated by the same subtraction in FP32 (within one ulp of
-// rounding the new FP64 state), which saves the FP64->FP32 conversions.
-__global__ void k_corvel_mixed(double* u1, double* u2, double* u3, float* v1, float* v2, float* v3, const float* p1,
-                               const float* p2, const float* p3, long long n) {
-  GRID_STRIDE(i, n) {
-    const float a = p1[i], b = p2[i], c = p3[i];
-    u1[i] = u1[i] - (double)a;
-    u2[i] = u2[i] - (double)b;
-    u3[i] = u3[i] - (double)c;
-    v1[i] = v1[i] - a;
-    v2[i] = v2[i] - b;
-    v3[i] = v3[i] - c;
   }
 }
 
@@ -222,10 +204,11 @@ struct SolverImpl {
   int itime = 0;            // completed steps
   int ntime = 3, nsub = 1;
   double adt[3] = {0, 0, 0}, bdt[3] = {0, 0, 0}, cdt[3] = {0, 0, 0}, gdt[3] = {0, 0, 0};
-  // FP64 state
+  // FP64 state (FP64 mode); staging for set/get/statistics (mixed mode)
   double *ux = nullptr, *uy = nullptr, *uz = nullptr;
-  // operator-precision copies of the state (mixed only)
-  float *ux32 = nullptr, *uy32 = nullptr, *uz32 = nullptr;
+  // mixed mode: double-float state (hi, lo); hi is the operators' FP32 input
+  float* uh[3] = {nullptr, nullptr, nullptr};
+  float* ul[3] = {nullptr, nullptr, nullptr};
   // history: [component][slot], precision of the operators
   void* H[3][3] = {{nullptr}};
   // work fields in operator precision
@@ -259,12 +242,27 @@ struct x3d_solver {
 namespace x3d {
 
 template <typename T>
-static int op(SolverImpl* s, int axis, int kind, int npaire, T* out, const T* in, const int* dims, cudaStream_t st) {
+static int op(SolverImpl* s, int axis, int kind, int npaire, T* out, const T* in, const int* dims, cudaStream_t st,
+              const Fuse<T>* fz = nullptr) {
   OpPlan* p = nullptr;
   int rc = get_plan(s->c, axis, kind, npaire, default_coefset(kind, npaire), &p);
   if (rc != X3D_OK) return rc;
   s->launches++;
-  return launch_line_op<T>(s->c, p, out, in, dims, nullptr, st);
+  return launch_line_op<T>(s->c, p, out, in, dims, nullptr, st, fz);
+}
+
+template <typename T>
+Fuse<T> fz_prod(const T* in2) {
+  Fuse<T> f;
+  f.in2 = in2;
+  return f;
+}
+template <typename T>
+Fuse<T> fz_comb(T cr, const T* a1, T c1, const T* a2, T c2, const T* y) {
+  Fuse<T> f;
+  f.cr = cr; f.a1 = a1; f.c1 = c1; f.a2 = a2; f.c2 = c2; f.y = y;
+  f.active = 1;
+  return f;
 }
 
 #define RC(x)                      \
@@ -274,73 +272,54 @@ static int op(SolverImpl* s, int axis, int kind, int npaire, T* out, const T* in
   } while (0)
 
 // momentum_rhs_eq (src/transeq.f90:73-591) for the incompressible periodic
-// case, in operator precision T; writes the new right-hand side into h1,h2,h3.
-template <typename T, typename H>
-static int momentum_rhs(SolverImpl* s, const T* ux, const T* uy, const T* uz, H* hx, H* hy, H* hz, cudaStream_t st) {
+// case, in operator precision T.  For each component u_q and direction j the
+// reference forms conv_j = d_j(u_q u_j) + u_j d_j u_q and nu d_jj u_q between
+// transposes; here every product is formed while a line kernel loads its
+// input and every sum while it stores its output, so the 27 line solves carry
+// all the pointwise work and no separate elementwise pass touches HBM:
+//   X: t1 = dx(ux*uq);   tg = t1 + ux*dx(uq)
+//   Y: t1 = dy(uy*uq);   th = t1 + uy*dy(uq)
+//   Z: t1 = dz(uz*uq);   tz = t1 + uz*dz(uq);   tz = nu*dzz(uq) - tz/2
+//   Y: tz = nu*dyy(uq) + tz - th/2
+//   X: H_q = nu*dxx(uq) + tz - tg/2
+// Parities follow the reference's calls: npaire = 0 for d_j u_j and d_jj u_j,
+// 1 for the other components (and the reverse for the products).
+template <typename T>
+static int momentum_rhs(SolverImpl* s, const T* const* u, T* const* H, cudaStream_t st) {
   Ctx* c = s->c;
-  const long long N = s->N;
   const int dims[3] = {c->grid.nx, c->grid.ny, c->grid.nz};
   T** w = reinterpret_cast<T**>(s->W);
-  T *ta = w[0], *tb = w[1], *tc = w[2], *td = w[3], *te = w[4], *tf = w[5];
-  T *tg1 = w[6], *th1 = w[7], *ti1 = w[8];
-  T *tg2 = w[9], *th2 = w[10], *ti2 = w[11];
-  const unsigned nb = pw_blocks(c, N);
+  T *t1 = w[0], *tg = w[1], *th = w[2], *tz = w[3];
   const T xnu = (T)s->o.xnu;
-  // X stage
-  k_prod3<T><<<nb, 256, 0, st>>>(ta, tb, tc, ux, uy, uz, ux, N);
-  s->launches++;
-  RC(op<T>(s, 0, K_DER1, 1, td, ta, dims, st));
-  RC(op<T>(s, 0, K_DER1, 0, te, tb, dims, st));
-  RC(op<T>(s, 0, K_DER1, 0, tf, tc, dims, st));
-  RC(op<T>(s, 0, K_DER1, 0, ta, ux, dims, st));
-  RC(op<T>(s, 0, K_DER1, 1, tb, uy, dims, st));
-  RC(op<T>(s, 0, K_DER1, 1, tc, uz, dims, st));
-  k_addmul3<T><<<nb, 256, 0, st>>>(tg1, th1, ti1, td, te, tf, ta, tb, tc, ux, N);
-  s->launches++;
-  // Y stage
-  k_prod3<T><<<nb, 256, 0, st>>>(td, te, tf, ux, uy, uz, uy, N);
-  s->launches++;
-  RC(op<T>(s, 1, K_DER1, 0, tg2, td, dims, st));
-  RC(op<T>(s, 1, K_DER1, 1, th2, te, dims, st));
-  RC(op<T>(s, 1, K_DER1, 0, ti2, tf, dims, st));
-  RC(op<T>(s, 1, K_DER1, 1, td, ux, dims, st));
-  RC(op<T>(s, 1, K_DER1, 0, te, uy, dims, st));
-  RC(op<T>(s, 1, K_DER1, 1, tf, uz, dims, st));
-  k_addmul3<T><<<nb, 256, 0, st>>>(tg2, th2, ti2, tg2, th2, ti2, td, te, tf, uy, N);
-  s->launches++;
-  // Z stage: products, first derivatives, convective sum
-  k_prod3<T><<<nb, 256, 0, st>>>(td, te, tf, ux, uy, uz, uz, N);
-  s->launches++;
-  RC(op<T>(s, 2, K_DER1, 0, ta, td, dims, st));
-  RC(op<T>(s, 2, K_DER1, 0, tb, te, dims, st));
-  RC(op<T>(s, 2, K_DER1, 1, tc, tf, dims, st));
-  RC(op<T>(s, 2, K_DER1, 1, td, ux, dims, st));
-  RC(op<T>(s, 2, K_DER1, 1, te, uy, dims, st));
-  RC(op<T>(s, 2, K_DER1, 0, tf, uz, dims, st));
-  // ta3 = tg3 + uz*td3 (conv z), stored in ta/tb/tc
-  k_addmul3<T><<<nb, 256, 0, st>>>(ta, tb, tc, ta, tb, tc, td, te, tf, uz, N);
-  s->launches++;
-  // derzz into td/te/tf, then td3 = xnu*derzz - 0.5*conv_z
-  RC(op<T>(s, 2, K_DER2, 1, td, ux, dims, st));
-  RC(op<T>(s, 2, K_DER2, 1, te, uy, dims, st));
-  RC(op<T>(s, 2, K_DER2, 0, tf, uz, dims, st));
-  k_lin3<T><<<nb, 256, 0, st>>>(ta, tb, tc, td, te, tf, ta, tb, tc, xnu, T(-0.5), N);
-  s->launches++;
-  // back to Y: tg2 = td3 - 0.5*tg2
-  k_lin3<T><<<nb, 256, 0, st>>>(tg2, th2, ti2, ta, tb, tc, tg2, th2, ti2, T(1), T(-0.5), N);
-  s->launches++;
-  RC(op<T>(s, 1, K_DER2, 1, td, ux, dims, st));
-  RC(op<T>(s, 1, K_DER2, 0, te, uy, dims, st));
-  RC(op<T>(s, 1, K_DER2, 1, tf, uz, dims, st));
-  // ta2 = xnu*td2 + tg2
-  k_lin3<T><<<nb, 256, 0, st>>>(tg2, th2, ti2, td, te, tf, tg2, th2, ti2, xnu, T(1), N);
-  s->launches++;
-  // back to X: second derivatives and the final sum
-  RC(op<T>(s, 0, K_DER2, 0, td, ux, dims, st));
-  RC(op<T>(s, 0, K_DER2, 1, te, uy, dims, st));
-  RC(op<T>(s, 0, K_DER2, 1, tf, uz, dims, st));
-  k_final3<T, H><<<nb, 256, 0, st>>>(hx, hy, hz, tg2, th2, ti2, tg1, th1, ti1, td, te, tf, xnu, N);
-  s->launches++;
+  const T one = T(1), mhalf = T(-0.5), zero = T(0);
+  for (int q = 0; q < 3; ++q) {
+    const T* uq = u[q];
+    const int pu[3] = {q == 0 ? 0 : 1, q == 1 ? 0 : 1, q == 2 ? 0 : 1};  // parity of d_j u_q
+    Fuse<T> f;
+    // X
+    f = fz_prod<T>(uq);
+    RC(op<T>(s, 0, K_DER1, 1 - pu[0], t1, u[0], dims, st, &f));
+    f = fz_comb<T>(zero, t1, one, nullptr, zero, u[0]);
+    RC(op<T>(s, 0, K_DER1, pu[0], tg, uq, dims, st, &f));
+    // Y
+    f = fz_prod<T>(uq);
+    RC(op<T>(s, 1, K_DER1, 1 - pu[1], t1, u[1], dims, st, &f));
+    f = fz_comb<T>(zero, t1, one, nullptr, zero, u[1]);
+    RC(op<T>(s, 1, K_DER1, pu[1], th, uq, dims, st, &f));
+    // Z
+    f = fz_prod<T>(uq);
+    RC(op<T>(s, 2, K_DER1, 1 - pu[2], t1, u[2], dims, st, &f));
+    f = fz_comb<T>(zero, t1, one, nullptr, zero, u[2]);
+    RC(op<T>(s, 2, K_DER1, pu[2], tz, uq, dims, st, &f));
+    f = fz_comb<T>(xnu, tz, mhalf, nullptr, zero, nullptr);
+    RC(op<T>(s, 2, K_DER2, pu[2], tz, uq, dims, st, &f));
+    // back to Y
+    f = fz_comb<T>(xnu, tz, one, th, mhalf, nullptr);
+    RC(op<T>(s, 1, K_DER2, pu[1], tz, uq, dims, st, &f));
+    // back to X: final sum into the history slot
+    f = fz_comb<T>(xnu, tz, one, tg, mhalf, nullptr);
+    RC(op<T>(s, 0, K_DER2, pu[0], H[q], uq, dims, st, &f));
+  }
   return cuda_status(cudaGetLastError());
 }
 
@@ -400,18 +379,13 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
   const long long N = s->N;
   const unsigned nb = pw_blocks(c, N);
   const bool mixed = std::is_same<T, float>::value;
-  const T* ux = mixed ? (const T*)s->ux32 : (const T*)s->ux;
-  const T* uy = mixed ? (const T*)s->uy32 : (const T*)s->uy;
-  const T* uz = mixed ? (const T*)s->uz32 : (const T*)s->uz;
-  T* hx = (T*)s->H[0][0];
-  T* hy = (T*)s->H[1][0];
-  T* hz = (T*)s->H[2][0];
-  RC((momentum_rhs<T, T>(s, ux, uy, uz, hx, hy, hz, st)));
+  // operator inputs: the FP64 state, or the hi part of the double-float state
+  const T* u[3];
+  for (int q = 0; q < 3; ++q) u[q] = mixed ? (const T*)s->uh[q] : (const T*)(q == 0 ? s->ux : q == 1 ? s->uy : s->uz);
+  T* H[3] = {(T*)s->H[0][0], (T*)s->H[1][0], (T*)s->H[2][0]};
+  RC(momentum_rhs<T>(s, u, H, st));
   // intt (src/time_integrators.f90:18-187); itime is the 1-based step index
   const int it = s->itime + 1;
-  double* U[3] = {s->ux, s->uy, s->uz};
-  float* U32[3] = {s->ux32, s->uy32, s->uz32};
-  // coefficients and number of history terms of this sub-step
   const double dt = s->o.dt;
   double c1 = 0, c2 = 0, c3 = 0;
   int nh = 1;
@@ -426,13 +400,14 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
   if (mixed) {
     Intt3 a;
     for (int q = 0; q < 3; ++q) {
-      a.u[q] = U[q];
-      a.u32[q] = U32[q];
+      a.uh[q] = s->uh[q];
+      a.ul[q] = s->ul[q];
       for (int k = 0; k < 3; ++k) a.h[q][k] = (const float*)s->H[q][k];
     }
-    k_intt_mixed<<<nb, 256, 0, st>>>(a, (float)c1, (float)c2, (float)c3, nh, N);
+    k_intt_df<<<nb, 256, 0, st>>>(a, (float)c1, (float)c2, (float)c3, nh, N);
     s->launches++;
   } else {
+    double* U[3] = {s->ux, s->uy, s->uz};
     for (int q = 0; q < 3; ++q) {
       k_intt64<<<nb, 256, 0, st>>>(U[q], (const double*)s->H[q][0], (const double*)s->H[q][1],
                                    (const double*)s->H[q][2], c1, c2, c3, nh, N);
@@ -453,27 +428,30 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
     }
   }
   RC(cuda_status(cudaGetLastError()));
-  // projection
-  const T* vx = mixed ? (const T*)s->ux32 : (const T*)s->ux;
-  const T* vy = mixed ? (const T*)s->uy32 : (const T*)s->uy;
-  const T* vz = mixed ? (const T*)s->uz32 : (const T*)s->uz;
-  RC(divergence<T>(s, vx, vy, vz, s->pp64, st));
+  // projection: divergence, Poisson, gradient, correction
+  RC(divergence<T>(s, u[0], u[1], u[2], s->pp64, st));
   // mixed: FP64-class Poisson solve in double-float arithmetic on the FP32 pipes
   RC(poisson_periodic(c, s->pp64, mixed ? 2 : 0, st));
   s->launches += 5;
   const T* pin = (const T*)s->pp64;
   T** w = reinterpret_cast<T**>(s->W);
   if (mixed) {
-    k_to32<<<pw_blocks(c, s->Np), 256, 0, st>>>((float*)w[12], s->pp64, s->Np);
+    k_to32<<<pw_blocks(c, s->Np), 256, 0, st>>>((float*)w[4], s->pp64, s->Np);
     s->launches++;
-    pin = (const T*)w[12];
+    pin = (const T*)w[4];
   }
   RC(gradp<T>(s, pin, w[0], w[1], w[2], st));
-  if (mixed)
-    k_corvel_mixed<<<nb, 256, 0, st>>>(s->ux, s->uy, s->uz, s->ux32, s->uy32, s->uz32, (const float*)w[0],
-                                       (const float*)w[1], (const float*)w[2], N);
-  else
+  if (mixed) {
+    Cor3 a;
+    for (int q = 0; q < 3; ++q) {
+      a.uh[q] = s->uh[q];
+      a.ul[q] = s->ul[q];
+      a.p[q] = (const float*)w[q];
+    }
+    k_corvel_df<<<nb, 256, 0, st>>>(a, N);
+  } else {
     k_corvel<T><<<nb, 256, 0, st>>>(s->ux, s->uy, s->uz, w[0], w[1], w[2], N);
+  }
   s->launches++;
   return cuda_status(cudaGetLastError());
 }
@@ -488,10 +466,11 @@ static int solver_alloc(SolverImpl* s) {
   s->uz = s->alloc<double>(N);
   if (!s->ux || !s->uy || !s->uz) return X3D_ERR_NOMEM;
   if (mixed) {
-    s->ux32 = s->alloc<float>(N);
-    s->uy32 = s->alloc<float>(N);
-    s->uz32 = s->alloc<float>(N);
-    if (!s->ux32 || !s->uy32 || !s->uz32) return X3D_ERR_NOMEM;
+    for (int q = 0; q < 3; ++q) {
+      s->uh[q] = s->alloc<float>(N);
+      s->ul[q] = s->alloc<float>(N);
+      if (!s->uh[q] || !s->ul[q]) return X3D_ERR_NOMEM;
+    }
   }
   for (int q = 0; q < 3; ++q)
     for (int k = 0; k < s->ntime; ++k) {
@@ -499,7 +478,7 @@ static int solver_alloc(SolverImpl* s) {
       if (!s->H[q][k]) return X3D_ERR_NOMEM;
       cudaMemset(s->H[q][k], 0, (size_t)N * es);
     }
-  for (int k = 0; k < 13; ++k) {
+  for (int k = 0; k < 5; ++k) {
     s->W[k] = s->alloc<unsigned char>(N * (long long)es);
     if (!s->W[k]) return X3D_ERR_NOMEM;
   }
@@ -558,14 +537,24 @@ int x3d_solver_destroy(x3d_solver* s) {
   return X3D_OK;
 }
 
+// After the FP64 staging arrays change: derive the double-float state.
 static int sync_copies(SolverImpl* s) {
   if (!s->mixed()) return X3D_OK;
   Ctx* c = s->c;
   const unsigned nb = pw_blocks(c, s->N);
-  k_to32<<<nb, 256>>>(s->ux32, s->ux, s->N);
-  k_to32<<<nb, 256>>>(s->uy32, s->uy, s->N);
-  k_to32<<<nb, 256>>>(s->uz32, s->uz, s->N);
+  const double* U[3] = {s->ux, s->uy, s->uz};
+  for (int q = 0; q < 3; ++q) k_split<<<nb, 256>>>(s->uh[q], s->ul[q], U[q], s->N);
   return cuda_status(cudaDeviceSynchronize());
+}
+
+// Before reading the FP64 staging arrays: rebuild them from the double-float state.
+static int stage64(SolverImpl* s, cudaStream_t st) {
+  if (!s->mixed()) return X3D_OK;
+  Ctx* c = s->c;
+  const unsigned nb = pw_blocks(c, s->N);
+  double* U[3] = {s->ux, s->uy, s->uz};
+  for (int q = 0; q < 3; ++q) k_combine<<<nb, 256, 0, st>>>(U[q], s->uh[q], s->ul[q], s->N);
+  return cuda_status(cudaGetLastError());
 }
 
 int x3d_solver_set_velocity(x3d_solver* s, const double* ux, const double* uy, const double* uz, int on_device) {
@@ -583,6 +572,8 @@ int x3d_solver_set_velocity(x3d_solver* s, const double* ux, const double* uy, c
 int x3d_solver_get_velocity(x3d_solver* s, double* ux, double* uy, double* uz, int on_device) {
   if (!s || !ux || !uy || !uz) return X3D_ERR_ARG;
   SolverImpl* si = &s->impl;
+  int rc = stage64(si, nullptr);
+  if (rc != X3D_OK) return rc;
   const size_t b = (size_t)si->N * sizeof(double);
   const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
   if (cudaMemcpy(ux, si->ux, b, k) != cudaSuccess || cudaMemcpy(uy, si->uy, b, k) != cudaSuccess ||
@@ -628,6 +619,8 @@ int x3d_solver_tgv_stats(x3d_solver* s, double* out, void* stream) {
   Ctx* c = si->c;
   cudaStream_t st = (cudaStream_t)stream;
   const int dims[3] = {c->grid.nx, c->grid.ny, c->grid.nz};
+  int rc0 = stage64(si, st);
+  if (rc0 != X3D_OK) return rc0;
   // 9 first + 9 second derivatives in FP64 (postprocess_tgv), in FP64 buffers
   std::vector<double*> g(9), l(9);
   double* buf = nullptr;
@@ -676,6 +669,8 @@ int x3d_solver_divmax(x3d_solver* s, double* out, void* stream) {
   SolverImpl* si = &s->impl;
   Ctx* c = si->c;
   cudaStream_t st = (cudaStream_t)stream;
+  int rc0 = stage64(si, st);
+  if (rc0 != X3D_OK) return rc0;
   // always evaluated in FP64 on the FP64 state
   double* tmp = nullptr;
   double* P[7];
