@@ -72,7 +72,7 @@ __device__ __forceinline__ T interior_w(const T* w, int k, const FastArgs<T>& p)
 }
 
 template <typename T, int KIND, bool XL, int L>
-__global__ void __launch_bounds__(LANES* FCHUNKS) line_fast(const __grid_constant__ FastArgs<T> p) {
+__global__ void __launch_bounds__(LANES* FCHUNKS, 2) line_fast(const __grid_constant__ FastArgs<T> p) {
   constexpr int LO = Halo<KIND>::lo, HI = Halo<KIND>::hi;
   constexpr int WN = L + LO + HI;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -206,10 +206,28 @@ __global__ void __launch_bounds__(LANES* FCHUNKS) line_fast(const __grid_constan
       const long long off = (long long)(a0 + lane) * p.sa + b * p.sb;
       T* dst = p.out + off;
       if (p.fz.active) {
+        // operands are read in groups of 8 rows before any store of the group:
+        // the output may alias a1/a2, so the compiler cannot batch them itself
+        constexpr int G = 4;
 #pragma unroll
-        for (int k = 0; k < L; ++k) {
-          const long long i = (long long)(r0 + k) * p.rs;
-          dst[i] = fuse_out(p.fz, v[k], off + i);
+        for (int k0 = 0; k0 < L; k0 += G) {
+          T A1[G], A2[G], Y[G];
+#pragma unroll
+          for (int g = 0; g < G; ++g) {
+            const long long i = off + (long long)(r0 + k0 + g) * p.rs;
+            A1[g] = p.fz.a1 ? p.fz.a1[i] : T(0);
+            A2[g] = p.fz.a2 ? p.fz.a2[i] : T(0);
+            Y[g] = p.fz.y ? p.fz.y[i] : T(0);
+          }
+#pragma unroll
+          for (int g = 0; g < G; ++g) {
+            const T t = v[k0 + g];
+            T o = (p.fz.cr != T(0)) ? p.fz.cr * t : T(0);
+            o = o + p.fz.c1 * A1[g];
+            o = o + p.fz.c2 * A2[g];
+            o = o + Y[g] * t;
+            dst[(long long)(r0 + k0 + g) * p.rs] = o;
+          }
         }
       } else {
 #pragma unroll

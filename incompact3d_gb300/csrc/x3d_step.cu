@@ -557,9 +557,38 @@ static int stage64(SolverImpl* s, cudaStream_t st) {
   return cuda_status(cudaGetLastError());
 }
 
+// Device-accessible address of a page-locked host buffer, or null.
+static const void* mapped_host(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (a.type == cudaMemoryTypeHost && a.devicePointer) ? a.devicePointer : nullptr;
+}
+
+__global__ void k_copy64(double* d, const double* s, long long n) {
+  GRID_STRIDE(i, n) d[i] = s[i];
+}
+
 int x3d_solver_set_velocity(x3d_solver* s, const double* ux, const double* uy, const double* uz, int on_device) {
   if (!s || !ux || !uy || !uz) return X3D_ERR_ARG;
   SolverImpl* si = &s->impl;
+  // Page-locked host buffers are read by the kernels directly (over the
+  // host-device link), without a staging copy.
+  if (!on_device) {
+    const void* m[3] = {mapped_host(ux), mapped_host(uy), mapped_host(uz)};
+    if (m[0] && m[1] && m[2]) {
+      const unsigned nb = pw_blocks(si->c, si->N);
+      double* U[3] = {si->ux, si->uy, si->uz};
+      for (int q = 0; q < 3; ++q) {
+        if (si->mixed()) k_split<<<nb, 256>>>(si->uh[q], si->ul[q], (const double*)m[q], si->N);
+        else k_copy64<<<nb, 256>>>(U[q], (const double*)m[q], si->N);
+      }
+      si->itime = 0;
+      return cuda_status(cudaDeviceSynchronize());
+    }
+  }
   const size_t b = (size_t)si->N * sizeof(double);
   const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   if (cudaMemcpy(si->ux, ux, b, k) != cudaSuccess || cudaMemcpy(si->uy, uy, b, k) != cudaSuccess ||
@@ -572,6 +601,18 @@ int x3d_solver_set_velocity(x3d_solver* s, const double* ux, const double* uy, c
 int x3d_solver_get_velocity(x3d_solver* s, double* ux, double* uy, double* uz, int on_device) {
   if (!s || !ux || !uy || !uz) return X3D_ERR_ARG;
   SolverImpl* si = &s->impl;
+  if (!on_device) {
+    void* m[3] = {(void*)mapped_host(ux), (void*)mapped_host(uy), (void*)mapped_host(uz)};
+    if (m[0] && m[1] && m[2]) {
+      const unsigned nb = pw_blocks(si->c, si->N);
+      double* U[3] = {si->ux, si->uy, si->uz};
+      for (int q = 0; q < 3; ++q) {
+        if (si->mixed()) k_combine<<<nb, 256>>>((double*)m[q], si->uh[q], si->ul[q], si->N);
+        else k_copy64<<<nb, 256>>>((double*)m[q], U[q], si->N);
+      }
+      return cuda_status(cudaDeviceSynchronize());
+    }
+  }
   int rc = stage64(si, nullptr);
   if (rc != X3D_OK) return rc;
   const size_t b = (size_t)si->N * sizeof(double);

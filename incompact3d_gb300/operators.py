@@ -228,13 +228,16 @@ class Solver:
             pass
 
     def set_velocity(self, ux, uy, uz):
-        """ux, uy, uz: numpy float64 (host) or torch CUDA float64 (device)."""
+        """ux, uy, uz: numpy float64 (host), contiguous torch CPU float64 (host;
+        page-locked ones are read by the kernels directly) or torch CUDA float64
+        (device)."""
         if isinstance(ux, np.ndarray):
             a = [np.ascontiguousarray(v, dtype=np.float64) for v in (ux, uy, uz)]
             check(self.lib.x3d_solver_set_velocity(self.h, *[v.ctypes.data_as(ctypes.c_void_p) for v in a], 0),
                   "x3d_solver_set_velocity")
         else:
-            check(self.lib.x3d_solver_set_velocity(self.h, _ptr(ux), _ptr(uy), _ptr(uz), 1),
+            on_dev = 1 if ux.is_cuda else 0
+            check(self.lib.x3d_solver_set_velocity(self.h, _ptr(ux), _ptr(uy), _ptr(uz), on_dev),
                   "x3d_solver_set_velocity")
 
     def get_velocity(self):
@@ -243,6 +246,15 @@ class Solver:
         check(self.lib.x3d_solver_get_velocity(self.h, *[v.ctypes.data_as(ctypes.c_void_p) for v in out], 0),
               "x3d_solver_get_velocity")
         return out
+
+    def get_velocity_into(self, ux, uy, uz):
+        """Copy the velocity into caller-provided host (numpy or pinned torch CPU)
+        or CUDA float64 arrays."""
+        def addr(a):
+            return a.ctypes.data_as(ctypes.c_void_p) if isinstance(a, np.ndarray) else ctypes.c_void_p(a.data_ptr())
+        on_dev = 0 if isinstance(ux, np.ndarray) or not getattr(ux, "is_cuda", False) else 1
+        check(self.lib.x3d_solver_get_velocity(self.h, addr(ux), addr(uy), addr(uz), on_dev),
+              "x3d_solver_get_velocity")
 
     def init_tgv(self):
         check(self.lib.x3d_solver_init_tgv(self.h), "x3d_solver_init_tgv")

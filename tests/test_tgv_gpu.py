@@ -73,3 +73,32 @@ def test_tgv_rk3_matches_oracle(oracle_mod, gpu_lib):
     _, _, _, rows_o, _ = o.run(ux, uy, uz, 20, 0.01, 1 / 1600.0, 5, 10)
     rows, s, ctx = run_gpu(gpu_lib, n, 20, 0.01, 5, gpu_lib.PREC_FP64)
     assert np.max(np.abs(rows[:, 1:] - rows_o[:, 1:]) / np.abs(rows_o[:, 1:])) < 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_pinned_host_transfer_matches_pageable(gpu_lib, precision):
+    """set/get with page-locked host buffers (read and written by kernels
+    directly) give the same velocity, bit for bit, as pageable numpy buffers."""
+    torch = pytest.importorskip("torch")
+    n = 32
+    ctx = gpu_lib.Context(n, n, n, L, L, L)
+    ic = tgv_ic(n)
+    res = []
+    for pinned in (False, True):
+        prec = gpu_lib.PREC_FP64 if precision == "fp64" else gpu_lib.PREC_MIXED
+        s = gpu_lib.Solver(ctx, 0.005, 1 / 1600.0, itimescheme=3, precision=prec)
+        if pinned:
+            h = [torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for v in ic]
+            s.set_velocity(*h)
+        else:
+            s.set_velocity(*ic)
+        s.step(3)
+        if pinned:
+            out = [torch.empty((n, n, n), dtype=torch.float64).pin_memory() for _ in range(3)]
+            s.get_velocity_into(*out)
+            out = [o.numpy() for o in out]
+        else:
+            out = s.get_velocity()
+        res.append(out)
+    for a, b in zip(*res):
+        assert np.array_equal(a, b)
