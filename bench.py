@@ -8,6 +8,7 @@ integration and Poisson FFT); the FP64 solver is reported beside it, together
 with the kinetic-energy difference between the two after the same steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--n 512] [--impl ours|reference]
+  python bench.py --workload ops [--n 512] [--ops dery,...] [--dtypes f64,f32] [--bcs 0,2]
 
 --impl reference times the CPU restatement of the reference's path (the
 parity oracle, C++/OpenMP on all host cores) on a bounded sample grid of the
@@ -27,6 +28,12 @@ sys.path.insert(0, ROOT)
 
 METRIC = "TGV 512^3 Mpts*steps/s (mixed FP32/FP64 step; FP64 step reported beside it)"
 UNIT = "Mpts*steps/s"
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum of one y-line FP32 first
+# derivative launch on the 512^3 field (ncu --set full capture of
+# `bench.py --workload ops --n 512 --ops dery --dtypes f32 --bcs 0 --reps 1`)
+DERY_F32_512_DRAM_BYTES = 1025895680
 
 
 def dist_env():
@@ -261,7 +268,8 @@ def run_ours(args):
         "e2e": e2e,
         "gpu_launches": int(main["launches"] * args.steps),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk, "unit": "GB/s",
-                     "frac": round(achieved / pk, 4), "traffic": None,
+                     "frac": round(achieved / pk, 4),
+                     "traffic": DERY_F32_512_DRAM_BYTES if n == 512 else None,
                      "kernel": "line_kernel<float,DER1> y-lines 512^3 (dery FP32)",
                      "peak_source": pk_kind},
         "cpu_baseline": {"value": round(cpu_rate, 4) if cpu_rate else None, "unit": UNIT, "cores": cpu_threads,
@@ -279,8 +287,96 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+def spectral_field(torch, n, L, periodic, seed=20261204, nmodes=64, kmax=32, zero_mean=False):
+    """Operator-microbench input on the device, shape (n, n, n), FP64:
+    f = sum_m A_m cos(k_m . x + phi_m), integer k_m with 1 <= |k| <= kmax
+    (components in [-kmax, kmax]), A_m = |k|^(-5/3) / sqrt(sum |k|^(-10/3)),
+    phi_m ~ U[0, 2pi); k drawn first, then the phases."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    ks = []
+    while len(ks) < nmodes:
+        k = rng.integers(-kmax, kmax + 1, size=3)
+        r = float(np.sqrt((k * k).sum()))
+        if 1 <= r <= kmax:
+            ks.append(k)
+    ph = rng.uniform(0, 2 * np.pi, size=nmodes)
+    amp = np.array([float(np.sqrt((k * k).sum())) ** (-5 / 3) for k in ks])
+    amp /= np.sqrt((amp ** 2).sum())
+    d = L / n if periodic else L / (n - 1)
+    x = torch.arange(n, dtype=torch.float64, device="cuda") * d
+    f = torch.zeros((n, n, n), dtype=torch.float64, device="cuda")
+    for k, a, p in zip(ks, amp, ph):
+        # k . x for the (z, y, x) index order
+        arg = (k[2] * x)[:, None, None] + (k[1] * x)[None, :, None] + (k[0] * x)[None, None, :] + p
+        f += a * torch.cos(arg)
+    if zero_mean:
+        f -= f.mean()
+    return f
+
+
+def run_ops(args):
+    """Operator microbench: compact first/second derivatives and the filter
+    along x, y and z on n^3 fields, FP64 and FP32, periodic (ncl=0) and
+    Dirichlet (ncl=2) boundaries, plus the FFT Poisson solve on a zero-mean
+    RHS; one JSON line per case with GB/s against the HBM peak (algorithmic
+    bytes (N_in + N_out) * element size; inputs larger than L2)."""
+    import numpy as np
+    import torch
+    import incompact3d_gb300 as x3d
+
+    x3d.build()
+    n = args.n
+    L = 2 * np.pi
+    N = n ** 3
+    stream = torch.cuda.current_stream()
+    pk, pk_kind = peaks()
+    want = set(args.ops.split(",")) if args.ops else None
+    names = {(x3d.OP_DER1, 0): "derx", (x3d.OP_DER1, 1): "dery", (x3d.OP_DER1, 2): "derz",
+             (x3d.OP_DER2, 0): "derxx", (x3d.OP_DER2, 1): "deryy", (x3d.OP_DER2, 2): "derzz",
+             (x3d.OP_FIL, 0): "filx", (x3d.OP_FIL, 1): "fily", (x3d.OP_FIL, 2): "filz"}
+    for bc in [int(b) for b in args.bcs.split(",")]:
+        ctx = x3d.Context(n, n, n, L, L, L, bc=((bc, bc),) * 3)
+        f64 = spectral_field(torch, n, L, bc == 0)
+        for dt in args.dtypes.split(","):
+            u = f64 if dt == "f64" else f64.float()
+            o = torch.empty_like(u)
+            es = u.element_size()
+            for (op, axis), nm in names.items():
+                if want and nm not in want:
+                    continue
+                npaire = 1 if op == x3d.OP_DER2 or op == x3d.OP_FIL else 0
+                sec = time_kernel(torch, lambda: ctx.apply(axis, op, npaire, u, out=o), args.reps, stream)
+                gbs = 2 * N * es / sec / 1e9
+                print(json.dumps({"op": nm, "dtype": dt, "ncl": bc, "n": n, "ms": round(1e3 * sec, 4),
+                                  "gbs": round(gbs, 1), "frac": round(gbs / pk, 4), "peak_source": pk_kind}),
+                      flush=True)
+            del u, o
+        del ctx, f64
+    if want is None or "poisson" in want:
+        ctx = x3d.Context(n, n, n, L, L, L)
+        rhs0 = spectral_field(torch, n, L, True, zero_mean=True)
+        rhs = torch.empty_like(rhs0)
+        for prec, nm in ((0, "fp64"), (2, "double-float"), (1, "fp32")):
+            def solve():
+                rhs.copy_(rhs0)
+                ctx.poisson(rhs, precision=prec)
+            copy_sec = time_kernel(torch, lambda: rhs.copy_(rhs0), args.reps, stream)
+            sec = time_kernel(torch, solve, args.reps, stream) - copy_sec
+            gbs = 2 * N * 8 / sec / 1e9
+            print(json.dumps({"op": "poisson_000", "arith": nm, "n": n, "ms": round(1e3 * sec, 4),
+                              "gbs": round(gbs, 1), "frac": round(gbs / pk, 4), "peak_source": pk_kind}),
+                  flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "ops"],
+                    help="tgv: the time-step benchmark (default); ops: operator microbench lines")
+    ap.add_argument("--ops", default="", help="ops workload: comma list (derx,...,filz,poisson)")
+    ap.add_argument("--dtypes", default="f64,f32")
+    ap.add_argument("--bcs", default="0,2")
+    ap.add_argument("--reps", type=int, default=10)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
@@ -295,7 +391,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.workload == "ops":
+        run_ops(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
