@@ -55,6 +55,9 @@ def _load():
             lib.ox_tgv_stats.argtypes = [P, D, D, D, ctypes.c_double, D]
             lib.ox_run.argtypes = [P, D, D, D, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_int, ctypes.c_int, D, D]
+            lib.ox_stretching.argtypes = [P, ctypes.c_int, D]
+            lib.ox_run_channel.argtypes = [P, D, D, D, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_int, ctypes.c_double, ctypes.c_int, D, D]
             _lib = lib
     return _lib
 
@@ -72,13 +75,14 @@ class Oracle:
 
     def __init__(self, nx, ny, nz, xlx, yly, zlz, bc=((0, 0), (0, 0), (0, 0)),
                  ifirstder=4, isecondder=4, ipinter=3, filter_alpha=0.49,
-                 nu0nu=4.0, cnu=0.44):
+                 nu0nu=4.0, cnu=0.44, istret=0, beta=0.0):
         self.lib = _load()
         self.nx, self.ny, self.nz = nx, ny, nz
         self.bc = bc
-        iv = (ctypes.c_int * 12)(nx, ny, nz, bc[0][0], bc[0][1], bc[1][0], bc[1][1],
-                                  bc[2][0], bc[2][1], ifirstder, isecondder, ipinter)
-        dv = (ctypes.c_double * 6)(xlx, yly, zlz, filter_alpha, nu0nu, cnu)
+        self.istret = istret
+        iv = (ctypes.c_int * 13)(nx, ny, nz, bc[0][0], bc[0][1], bc[1][0], bc[1][1],
+                                  bc[2][0], bc[2][1], ifirstder, isecondder, ipinter, istret)
+        dv = (ctypes.c_double * 7)(xlx, yly, zlz, filter_alpha, nu0nu, cnu, beta)
         self.h = self.lib.ox_create(iv, dv)
         self.n = (nx, ny, nz)
         self.nm = tuple(n if b == (0, 0) else n - 1 for n, b in zip(self.n, bc))
@@ -164,3 +168,29 @@ class Oracle:
                             every, _dp(stats), _dp(dmax))
         assert n >= 0, n
         return ux, uy, uz, stats[:n], float(dmax[0])
+
+    STRETCH_NAMES = ("yp", "ypi", "ppy", "pp2y", "pp4y", "ppyi", "pp2yi", "pp4yi")
+
+    def stretching(self):
+        """Mesh metrics of src/stretching.f90 (dict of arrays) plus alpha."""
+        out = {}
+        buf = np.zeros(self.ny + 8)
+        for w, nm in enumerate(self.STRETCH_NAMES):
+            n = self.lib.ox_stretching(self.h, w, _dp(buf))
+            out[nm] = buf[:n].copy()
+        self.lib.ox_stretching(self.h, 8, _dp(buf))
+        out["alpha"] = float(buf[0])
+        return out
+
+    def run_channel(self, ux, uy, uz, nsteps, dt, xnu, itimescheme=5, wrotation=0.0, spinup_time=0):
+        """Channel time loop (constant flow rate, no-slip walls in y); returns the
+        velocity, the bulk velocity seen by the flow-rate correction at every
+        sub-step, and max|div u| at the end."""
+        ux, uy, uz = _c64(ux).copy(), _c64(uy).copy(), _c64(uz).copy()
+        nsub = 3 if itimescheme == 5 else 1
+        ub = np.zeros(nsteps * nsub)
+        dmax = np.zeros(1)
+        n = self.lib.ox_run_channel(self.h, _dp(ux), _dp(uy), _dp(uz), nsteps, dt, xnu, itimescheme,
+                                    wrotation, spinup_time, _dp(ub), _dp(dmax))
+        assert n >= 0, n
+        return ux, uy, uz, ub[:n], float(dmax[0])

@@ -738,10 +738,15 @@ struct OxCtx {
   double xlx, yly, zlz;
   Opts opts;
   Axis ax[3];
-  vec ppy;  // stretching metric (istret=0: ones)
+  // mesh stretching in y (src/stretching.f90:92-270); istret=0 leaves these empty
+  int istret = 0;
+  double beta = 0, alpha = 0;
+  vec yp, ypi, ppy, pp2y, pp4y, ppyi, pp2yi, pp4yi;
   // poisson_000 tables
   vec kx2, ky2, kz2, tx, ty, tz;  // per-axis modified wavenumber^2 and interpolation transfer
   vec sax, sbx, say, sby, saz, sbz;
+  // poisson_010 tables (x, z periodic; y non-periodic on nym points)
+  vec yky10, yk210, eys10, trx10, try10, trz10;
 };
 
 namespace {
@@ -799,6 +804,134 @@ void abxyz_axis(int n, vec& sa, vec& sb) {
 }
 
 inline size_t idx3(int i, int j, int k, int nx, int ny) { return (size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k); }
+
+// Mesh stretching in y: src/stretching.f90:92-270 (stretching_full) and the
+// uniform-mesh defaults of src/variables.f90:1294-1305 (ppy = 1, 2 at
+// non-periodic ends).  Fills yp, ypi, ppy, pp2y, pp4y, ppyi, pp2yi, pp4yi and
+// the mapping constant alpha.
+void stretching_setup(OxCtx& c) {
+  const int ny = c.ny;
+  const Axis& a = c.ax[1];
+  c.yp.assign(ny, 0.0); c.ypi.assign(ny, 0.0);
+  c.ppy.assign(ny, 1.0); c.pp2y.assign(ny, 0.0); c.pp4y.assign(ny, 0.0);
+  c.ppyi.assign(ny, 1.0); c.pp2yi.assign(ny, 0.0); c.pp4yi.assign(ny, 0.0);
+  if (c.istret == 0) {
+    for (int j = 0; j < ny; ++j) {
+      c.yp[j] = (double)j * a.d;
+      c.ypi[j] = ((double)(j + 1) - 0.5) * a.d;
+    }
+    if (a.ncl1 == 1 || a.ncl1 == 2) c.ppy[0] = 2.0;
+    if (a.ncln == 1 || a.ncln == 2) c.ppy[ny - 1] = 2.0;
+    return;
+  }
+  const int istret = c.istret;
+  const double beta = c.beta, yly = c.yly;
+  const int nym = a.periodic ? ny : ny - 1;
+  vec yeta(ny, 0.0), yetai(ny, 0.0);
+  const double yinf = -yly / 2.0;
+  double den = 2.0 * beta * yinf;
+  double xnum = -yinf - std::sqrt(PI * PI * beta * beta + yinf * yinf);
+  const double alpha = std::fabs(xnum / den);
+  c.alpha = alpha;
+  auto mapped = [&](double ye) {
+    const double den1 = std::sqrt(alpha * beta + 1.0);
+    const double xn = den1 / std::sqrt(alpha / PI) / std::sqrt(beta) / std::sqrt(PI);
+    const double dn = 2.0 * std::sqrt(alpha / PI) * std::sqrt(beta) * PI * std::sqrt(PI);
+    const double den3 = ((std::sin(PI * ye)) * (std::sin(PI * ye)) / beta / PI) + alpha / PI;
+    const double den4 = 2.0 * alpha * beta - std::cos(2.0 * PI * ye) + 1.0;
+    const double xnum1 = (std::atan(xn * std::tan(PI * ye))) * den4 / den1 / den3 / dn;
+    const double cst = std::sqrt(beta) * PI / (2.0 * std::sqrt(alpha) * std::sqrt(alpha * beta + 1.0));
+    double y = 0.0;
+    if (istret == 1) {
+      if (ye < 0.5) y = xnum1 - cst - yinf;
+      if (ye == 0.5) y = 0.0 - yinf;
+      if (ye > 0.5) y = xnum1 + cst - yinf;
+    } else if (istret == 2) {
+      if (ye < 0.5) y = xnum1 - cst + yly;
+      if (ye == 0.5) y = 0.0 + yly;
+      if (ye > 0.5) y = xnum1 + cst + yly;
+    } else {
+      if (ye < 0.5) y = (xnum1 - cst + yly) * 2.0;
+      if (ye == 0.5) y = (0.0 + yly) * 2.0;
+      if (ye > 0.5) y = (xnum1 + cst + yly) * 2.0;
+    }
+    return y;
+  };
+  if (alpha != 0.0) {
+    c.yp[0] = 0.0;
+    yeta[0] = (istret == 1) ? 0.0 : -0.5;
+    for (int j = 2; j <= ny; ++j) {
+      if (istret == 1) yeta[j - 1] = (double)(j - 1) * (1.0 / (double)nym);
+      if (istret == 2) yeta[j - 1] = (double)(j - 1) * (1.0 / (double)nym) - 0.5;
+      if (istret == 3) yeta[j - 1] = (double)(j - 1) * (0.5 / (double)nym) - 0.5;
+      c.yp[j - 1] = mapped(yeta[j - 1]);
+    }
+    for (int j = 1; j <= ny; ++j) {
+      if (istret == 1) yetai[j - 1] = ((double)j - 0.5) * (1.0 / (double)nym);
+      if (istret == 2) yetai[j - 1] = ((double)j - 0.5) * (1.0 / (double)nym) - 0.5;
+      if (istret == 3) yetai[j - 1] = ((double)j - 0.5) * (0.5 / (double)nym) - 0.5;
+      c.ypi[j - 1] = mapped(yetai[j - 1]);
+    }
+  } else {
+    c.yp[0] = -1.e10;
+    for (int j = 2; j <= ny; ++j) {
+      yeta[j - 1] = (double)(j - 1) * (1.0 / (double)ny);
+      c.yp[j - 1] = -beta * std::cos(PI * yeta[j - 1]) / std::sin(yeta[j - 1] * PI);
+    }
+    c.ypi[0] = -1.e10;
+    for (int j = 2; j <= ny; ++j) {
+      yetai[j - 1] = (double)(j - 1) * (1.0 / (double)ny);
+      c.ypi[j - 1] = -beta * std::cos(PI * yetai[j - 1]) / std::sin(yetai[j - 1] * PI);
+    }
+  }
+  const double q = (istret == 3) ? 2.0 : 1.0;
+  for (int j = 0; j < ny; ++j) {
+    c.ppy[j] = yly * (alpha / PI + (1.0 / PI / beta) * std::sin(PI * yeta[j]) * std::sin(PI * yeta[j]));
+    c.pp2y[j] = c.ppy[j] * c.ppy[j];
+    c.pp4y[j] = (-2.0 / beta * std::cos(PI * yeta[j]) * std::sin(PI * yeta[j]));
+    if (istret == 3) c.pp4y[j] = c.pp4y[j] / q;
+    c.ppyi[j] = yly * (alpha / PI + (1.0 / PI / beta) * std::sin(PI * yetai[j]) * std::sin(PI * yetai[j]));
+    c.pp2yi[j] = c.ppyi[j] * c.ppyi[j];
+    c.pp4yi[j] = (-2.0 / beta * std::cos(PI * yetai[j]) * std::sin(PI * yetai[j]));
+    if (istret == 3) c.pp4yi[j] = c.pp4yi[j] / q;
+  }
+}
+
+// Wavenumbers of a non-periodic y axis for poisson_010: src/poisson.f90:1603-1619
+// (waves, bcy = 1) and the transfer function of src/poisson.f90:1663-1676.
+// yky, yk2, eys have ny (velocity-mesh) entries; the transfer has nym.
+void waves_y010(const OxCtx& c, vec& yky, vec& yk2, vec& eys, vec& tr) {
+  const Axis& a = c.ax[1];
+  const int ny = a.n, nym = a.nm;
+  yky.assign(ny, 0.0); yk2.assign(ny, 0.0); eys.assign(ny, 0.0); tr.assign(nym, 0.0);
+  for (int j = 1; j <= ny; ++j) {
+    const double w = TWOPI * 0.5 * (double)(j - 1) / (double)nym;
+    double wp = a.aci6 * 2.0 * a.d * std::sin(w * 0.5) + (a.bci6 * 2.0 * a.d) * std::sin(3.0 * 0.5 * w);
+    wp = wp / (1.0 + 2.0 * a.alcai6 * std::cos(w));
+    yky[j - 1] = (c.istret == 0) ? (double)nym * wp / c.yly : (double)nym * wp;
+    eys[j - 1] = (double)nym * w / c.yly;
+    const double t = (double)nym * wp / c.yly;
+    yk2[j - 1] = t * t;
+  }
+  yky[0] = 0.0; eys[0] = 0.0; yk2[0] = 0.0;
+  for (int j = 0; j < nym; ++j) {
+    const double rl = eys[j] * a.d;
+    const double tt = 2.0 * (a.bici6 * std::cos(rl * 1.5) + a.cicoef6 * std::cos(rl * 2.5) + a.dici6 * std::cos(rl * 3.5));
+    const double tt1 = 2.0 * a.aici6 * std::cos(rl * 0.5);
+    const double t1 = 1.0 + 2.0 * a.ailcai6 * std::cos(rl);
+    tr[j] = (tt1 + tt) / t1;
+  }
+}
+
+// abxyz, non-periodic branch: src/poisson.f90:1489-1496.
+void abxyz_half(int n, vec& sa, vec& sb) {
+  sa.assign(n, 0.0);
+  sb.assign(n, 0.0);
+  for (int i = 1; i <= n; ++i) {
+    sa[i - 1] = std::sin((double)(i - 1) * PI * 0.5 / (double)n);
+    sb[i - 1] = std::cos((double)(i - 1) * PI * 0.5 / (double)n);
+  }
+}
 
 // Apply operator `op` along `axis` to the 3-D field u (dims nin along the axis),
 // writing t (dims nout along the axis).  dims[] are the input dims.
@@ -946,6 +1079,322 @@ static void poisson_000(const OxCtx& c, double* rhs) {
 }
 
 // ---------------------------------------------------------------------------
+// Poisson solve with x and z periodic and y non-periodic (Neumann):
+// src/poisson.f90:665-1013 (poisson_010), spectral array (nx, nym, nz/2+1)
+// as 2DECOMP's PHYSICAL_IN_Z transform leaves it.
+// ---------------------------------------------------------------------------
+
+// Pentadiagonal systems of src/poisson.f90:1814-2113 (matrice_refinement,
+// istret = 1 or 2, bcz = 0).  With x and z periodic every coefficient of the
+// reference is cx_one_one times a real number, so the real value is kept and
+// serves both the real and the imaginary solve.  Layout: d[q][i + nx*(m + nh*k)].
+struct Penta {
+  int nx = 0, nh = 0, nk = 0;
+  vec d[5];
+  double& at(int q, int i, int m, int k) { return d[q][(size_t)i + (size_t)nx * ((size_t)m + (size_t)nh * k)]; }
+  double at(int q, int i, int m, int k) const { return d[q][(size_t)i + (size_t)nx * ((size_t)m + (size_t)nh * k)]; }
+};
+
+void matrice_refinement(const OxCtx& c, Penta& A, Penta& A2) {
+  const int nx = c.nx, nym = c.ax[1].nm, nz2 = c.nz / 2 + 1, nh = nym / 2;
+  for (Penta* P : {&A, &A2}) {
+    P->nx = nx; P->nh = nh; P->nk = nz2;
+    for (int q = 0; q < 5; ++q) P->d[q].assign((size_t)nx * nh * nz2, 0.0);
+  }
+  const double alpha = c.alpha, beta = c.beta;
+  const double xa0 = alpha / PI + 0.5 / beta / PI;
+  const double xa1 = (c.istret == 1) ? 1.0 / 4.0 / beta / PI : -(1.0 / 4.0 / beta / PI);
+  const double xa0_2 = xa0 * xa0, xa1_2 = xa1 * xa1, xa01 = xa0 * xa1, xa0p1_2 = (xa0 + xa1) * (xa0 + xa1);
+  const vec &kx2 = c.kx2, &kz2 = c.kz2, &tx = c.trx10, &tz = c.trz10, &ty = c.try10, &yky = c.yky10;
+  auto ty2 = [&](int j1) { return ty[j1 - 1] * ty[j1 - 1]; };  // transy_rl2, 1-based
+  vec c1(nh + 2), c2(nh + 2);                                   // cw22 / cw2, 1-based
+  for (int k = 0; k < nz2; ++k)
+    for (int i = 0; i < nx; ++i) {
+      const double tx2 = tx[i] * tx[i], tz2 = tz[k] * tz[k];
+      for (int j = 1; j <= nh; ++j) {
+        c1[j] = tx[i] * (yky[2 * j - 2] * tz[k]);
+        c2[j] = tx[i] * (yky[2 * j - 1] * tz[k]);
+      }
+      auto diag = [&](int jy, double cc, double a2c, double nb) {
+        return -(kx2[i] * ty2(jy) * tz2 + kz2[k] * ty2(jy) * tx2 + a2c * (cc * cc) + xa1_2 * cc * nb);
+      };
+      // main diagonal
+      for (int j = 2; j <= nh - 1; ++j) {
+        A.at(2, i, j - 1, k) = diag(2 * j - 1, c1[j], xa0_2, c1[j - 1] + c1[j + 1]);
+        A2.at(2, i, j - 1, k) = diag(2 * j, c2[j], xa0_2, c2[j - 1] + c2[j + 1]);
+      }
+      A.at(2, i, 0, k) = diag(1, c1[1], xa0_2, c1[2]);
+      A.at(2, i, nh - 1, k) = diag(2 * nh - 1, c1[nh], xa0_2, c1[nh - 1]);
+      A2.at(2, i, 0, k) = diag(2, c2[1], xa0_2 - xa1_2, c2[2]);
+      A2.at(2, i, nh - 1, k) = diag(2 * nh, c2[nh], xa0p1_2, c2[nh - 1]);
+      // super-diagonal +1
+      for (int j = 2; j <= nh - 1; ++j) {
+        A.at(3, i, j - 1, k) = xa01 * (c1[j + 1] * (c1[j] + c1[j + 1]));
+        A2.at(3, i, j - 1, k) = xa01 * (c2[j + 1] * (c2[j] + c2[j + 1]));
+      }
+      A.at(3, i, 0, k) = 2.0 * xa01 * (c1[1] * c1[2] + c1[2] * c1[2]);
+      A2.at(3, i, 0, k) = (xa0 - xa1) * xa1 * (c2[1] * c2[2]) + xa0 * xa1 * (c2[2] * c2[2]);
+      A2.at(3, i, nh - 2, k) = xa0 * xa1 * c2[nh - 1] * c2[nh] + (xa0 + xa1) * xa1 * (c2[nh] * c2[nh]);
+      A2.at(3, i, nh - 1, k) = 0.0;
+      // super-diagonal +2
+      for (int j = 1; j <= nh - 2; ++j) {
+        A.at(4, i, j - 1, k) = xa1_2 * (-(c1[j + 1] * c1[j + 2]));
+        A2.at(4, i, j - 1, k) = xa1_2 * (-(c2[j + 1] * c2[j + 2]));
+      }
+      A.at(4, i, 0, k) = 2.0 * A.at(4, i, 0, k);
+      A.at(4, i, nh - 2, k) = 0.0; A.at(4, i, nh - 1, k) = 0.0;
+      A2.at(4, i, nh - 2, k) = 0.0; A2.at(4, i, nh - 1, k) = 0.0;
+      // sub-diagonal -1
+      for (int j = 2; j <= nh; ++j) {
+        A.at(1, i, j - 1, k) = xa01 * (c1[j - 1] * (c1[j] + c1[j - 1]));
+        A2.at(1, i, j - 1, k) = xa01 * (c2[j - 1] * (c2[j] + c2[j - 1]));
+      }
+      A.at(1, i, 0, k) = 0.0; A2.at(1, i, 0, k) = 0.0;
+      A2.at(1, i, 1, k) = xa0 * xa1 * (c2[2] * c2[1]) + (xa0 + xa1) * xa1 * (c2[1] * c2[1]);
+      A2.at(1, i, nh - 1, k) = (xa0 + xa1) * xa1 * (c2[nh] * c2[nh - 1]) + xa0 * xa1 * (c2[nh - 1] * c2[nh - 1]);
+      // sub-diagonal -2
+      for (int j = 3; j <= nh; ++j) {
+        A.at(0, i, j - 1, k) = xa1_2 * (-(c1[j - 1] * c1[j - 2]));
+        A2.at(0, i, j - 1, k) = xa1_2 * (-(c2[j - 1] * c2[j - 2]));
+      }
+      A.at(0, i, 0, k) = 0.0; A.at(0, i, 1, k) = 0.0;
+      A2.at(0, i, 0, k) = 0.0; A2.at(0, i, 1, k) = 0.0;
+      // the (kx, kz) = (0, 0) line: pin the first odd mode (no singular matrix)
+      if (kx2[i] == 0.0 && kz2[k] == 0.0) {
+        A.at(2, i, 0, k) = 1.0; A.at(3, i, 0, k) = 0.0; A.at(4, i, 0, k) = 0.0;
+      }
+    }
+}
+
+// src/tools.f90:1225-1362 (inversion5_v1): banded Gaussian elimination of the
+// pentadiagonal systems, real and imaginary parts separately (here with the
+// same real matrix).  Loop order and the epsilon guards follow the reference;
+// the pivots of the forward sweep are non-zero for these matrices.
+void inversion5_v1(const Penta& Ain, std::vector<cplx>& e, int nx, int nk) {
+  Penta a = Ain;
+  const int nh = a.nh;
+  const double eps = 1.0e-16;
+  auto E = [&](int i, int m, int k) -> cplx& { return e[(size_t)i + (size_t)nx * ((size_t)m + (size_t)nh * k)]; };
+  vec sr((size_t)nx * nk);
+  double tmp1 = 0, tmp2 = 0;
+  const int ja[2] = {3, 2}, jb[2] = {4, 3};  // 1-based diagonal indices
+  for (int m = 1; m <= nh - 2; ++m)
+    for (int ii = 1; ii <= 2; ++ii) {
+      const int mi = m + ii;
+      for (int k = 0; k < nk; ++k)
+        for (int j = 0; j < nx; ++j) {
+          const double piv = a.at(2, j, m - 1, k);
+          if (piv != 0.0) tmp1 = a.at(2 - ii, j, mi - 1, k) / piv;
+          if (piv != 0.0) tmp2 = a.at(2 - ii, j, mi - 1, k) / piv;
+          sr[(size_t)j + (size_t)nx * k] = tmp1;
+          const cplx em = E(j, m - 1, k), emi = E(j, mi - 1, k);
+          E(j, mi - 1, k) = cplx(emi.real() - tmp1 * em.real(), emi.imag() - tmp2 * em.imag());
+        }
+      for (int jc = ja[ii - 1]; jc <= jb[ii - 1]; ++jc)
+        for (int k = 0; k < nk; ++k)
+          for (int j = 0; j < nx; ++j)
+            a.at(jc - 1, j, mi - 1, k) =
+                a.at(jc - 1, j, mi - 1, k) - sr[(size_t)j + (size_t)nx * k] * a.at(jc + ii - 1, j, m - 1, k);
+    }
+  for (int k = 0; k < nk; ++k)
+    for (int j = 0; j < nx; ++j) {
+      const double p1 = a.at(2, j, nh - 2, k);
+      const double s = (std::fabs(p1) > eps) ? a.at(1, j, nh - 1, k) / p1 : 0.0;
+      const double b1 = a.at(2, j, nh - 1, k) - s * a.at(3, j, nh - 2, k);
+      const cplx en = E(j, nh - 1, k), en1 = E(j, nh - 2, k);
+      double t3r = 0, t3i = 0;
+      if (std::fabs(b1) > eps) {
+        const double t1 = s / b1;
+        t3r = en.real() / b1 - t1 * en1.real();
+        t3i = en.imag() / b1 - t1 * en1.imag();
+      }
+      E(j, nh - 1, k) = cplx(t3r, t3i);
+      const double r = (std::fabs(p1) > eps) ? 1.0 / p1 : 0.0;
+      const double a1 = a.at(3, j, nh - 2, k) * r;
+      const cplx enew = E(j, nh - 1, k);
+      E(j, nh - 2, k) = cplx(en1.real() * r - a1 * enew.real(), en1.imag() * r - a1 * enew.imag());
+    }
+  for (int i = nh - 2; i >= 1; --i)
+    for (int k = 0; k < nk; ++k)
+      for (int j = 0; j < nx; ++j) {
+        const double p = a.at(2, j, i - 1, k);
+        const double r = (std::fabs(p) > eps) ? 1.0 / p : 0.0;
+        const double a1 = a.at(3, j, i - 1, k) * r;
+        const double b1 = a.at(4, j, i - 1, k) * r;
+        const cplx e0 = E(j, i - 1, k), e1 = E(j, i, k), e2 = E(j, i + 1, k);
+        E(j, i - 1, k) = cplx(e0.real() * r - a1 * e1.real() - b1 * e2.real(),
+                              e0.imag() * r - a1 * e1.imag() - b1 * e2.imag());
+      }
+}
+
+static void poisson_010(const OxCtx& c, double* rhs) {
+  const int nx = c.nx, ny = c.ax[1].nm, nz = c.nz, nz2 = nz / 2 + 1, nh = ny / 2;
+  const size_t N = (size_t)nx * ny * nz;
+  // even/odd reorder in y (src/poisson.f90:688-698)
+  {
+    vec t(rhs, rhs + N);
+    for (int k = 0; k < nz; ++k)
+      for (int i = 0; i < nx; ++i) {
+        for (int j = 1; j <= ny / 2; ++j) rhs[idx3(i, j - 1, k, nx, ny)] = t[idx3(i, 2 * (j - 1), k, nx, ny)];
+        for (int j = ny / 2 + 1; j <= ny; ++j) rhs[idx3(i, j - 1, k, nx, ny)] = t[idx3(i, 2 * ny - 2 * j + 1, k, nx, ny)];
+      }
+  }
+  std::vector<cplx> cw((size_t)nx * ny * nz2);
+  auto CW = [&](int i, int j, int k) -> cplx& { return cw[(size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)]; };
+#pragma omp parallel
+  {
+    std::vector<cplx> line, work;
+#pragma omp for collapse(2)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        line.assign(nz, cplx(0, 0));
+        for (int k = 0; k < nz; ++k) line[k] = cplx(rhs[idx3(i, j, k, nx, ny)], 0.0);
+        fft1d(line.data(), nz, -1, work);
+        for (int k = 0; k < nz2; ++k) CW(i, j, k) = line[k];
+      }
+#pragma omp for collapse(2)
+    for (int k = 0; k < nz2; ++k)
+      for (int i = 0; i < nx; ++i) {
+        line.resize(ny);
+        for (int j = 0; j < ny; ++j) line[j] = CW(i, j, k);
+        fft1d(line.data(), ny, -1, work);
+        for (int j = 0; j < ny; ++j) CW(i, j, k) = line[j];
+      }
+#pragma omp for collapse(2)
+    for (int k = 0; k < nz2; ++k)
+      for (int j = 0; j < ny; ++j) {
+        line.resize(nx);
+        for (int i = 0; i < nx; ++i) line[i] = CW(i, j, k);
+        fft1d(line.data(), nx, -1, work);
+        for (int i = 0; i < nx; ++i) CW(i, j, k) = line[i];
+      }
+  }
+  for (auto& v : cw) v = cplx(v.real() / (double)nx / (double)ny / (double)nz, v.imag() / (double)nx / (double)ny / (double)nz);
+  // post-processing in z and x
+  for (int k = 0; k < nz2; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        cplx& v = CW(i, j, k);
+        double t1 = v.real(), t2 = v.imag();
+        v = cplx(t1 * c.sbz[k] + t2 * c.saz[k], t2 * c.sbz[k] - t1 * c.saz[k]);
+        t1 = v.real(); t2 = v.imag();
+        v = cplx(t1 * c.sbx[i] + t2 * c.sax[i], t2 * c.sbx[i] - t1 * c.sax[i]);
+        if (i + 1 > nx / 2 + 1) v = -v;
+      }
+  // post-processing in y (src/poisson.f90:764-785)
+  std::vector<cplx> cb(cw.size());
+  auto CB = [&](int i, int j, int k) -> cplx& { return cb[(size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)]; };
+  for (int k = 0; k < nz2; ++k)
+    for (int i = 0; i < nx; ++i) {
+      CB(i, 0, k) = CW(i, 0, k);
+      for (int j = 2; j <= ny; ++j) {
+        const double t1 = CW(i, j - 1, k).real(), t2 = CW(i, j - 1, k).imag();
+        const double t3 = CW(i, ny - j + 1, k).real(), t4 = CW(i, ny - j + 1, k).imag();
+        const double by = c.sby[j - 1], ay = c.say[j - 1];
+        const double x1 = t1 * by, x2 = t1 * ay, x3 = t2 * by, x4 = t2 * ay;
+        const double x5 = t3 * by, x6 = t3 * ay, x7 = t4 * by, x8 = t4 * ay;
+        CB(i, j - 1, k) = cplx(0.5 * (x1 + x4 + x5 - x8), 0.5 * (-x2 + x3 + x6 + x7));
+      }
+    }
+  if (c.istret == 0) {
+    const double eps = 1.0e-16;
+    for (int k = 0; k < nz2; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const double pyz = c.try10[j] * c.trz10[k], pxz = c.trx10[i] * c.trz10[k], pxy = c.trx10[i] * c.try10[j];
+          const double kk = c.kx2[i] * (pyz * pyz) + c.yk210[j] * (pxz * pxz) + c.kz2[k] * (pxy * pxy);
+          cplx& v = CB(i, j, k);
+          if (std::fabs(kk) < eps) v = cplx(0.0, 0.0);
+          else v = cplx(v.real() / (-kk), v.imag() / (-kk));
+        }
+  } else {
+    Penta A, A2;
+    matrice_refinement(c, A, A2);
+    std::vector<cplx> odd((size_t)nx * nh * nz2), even(odd.size());
+    for (int k = 0; k < nz2; ++k)
+      for (int j = 1; j <= nh; ++j)
+        for (int i = 0; i < nx; ++i) {
+          odd[(size_t)i + (size_t)nx * ((size_t)(j - 1) + (size_t)nh * k)] = CB(i, 2 * j - 2, k);
+          even[(size_t)i + (size_t)nx * ((size_t)(j - 1) + (size_t)nh * k)] = CB(i, 2 * j - 1, k);
+        }
+    inversion5_v1(A, odd, nx, nz2);
+    inversion5_v1(A2, even, nx, nz2);
+    for (int k = 0; k < nz2; ++k)
+      for (int j = 1; j <= nh; ++j)
+        for (int i = 0; i < nx; ++i) {
+          CB(i, 2 * j - 2, k) = odd[(size_t)i + (size_t)nx * ((size_t)(j - 1) + (size_t)nh * k)];
+          CB(i, 2 * j - 1, k) = even[(size_t)i + (size_t)nx * ((size_t)(j - 1) + (size_t)nh * k)];
+        }
+  }
+  for (int j = 0; j < ny; ++j) CB(nx / 2, j, nz / 2) = cplx(0.0, 0.0);
+  // backward post-processing in y (src/poisson.f90:907-929)
+  for (int k = 0; k < nz2; ++k)
+    for (int i = 0; i < nx; ++i) {
+      CW(i, 0, k) = CB(i, 0, k);
+      for (int j = 2; j <= ny; ++j) {
+        const double t1 = CB(i, j - 1, k).real(), t2 = CB(i, j - 1, k).imag();
+        const double t3 = CB(i, ny - j + 1, k).real(), t4 = CB(i, ny - j + 1, k).imag();
+        const double by = c.sby[j - 1], ay = c.say[j - 1];
+        const double x1 = t1 * by, x2 = t1 * ay, x3 = t2 * by, x4 = t2 * ay;
+        const double x5 = t3 * by, x6 = t3 * ay, x7 = t4 * by, x8 = t4 * ay;
+        CW(i, j - 1, k) = cplx(x1 - x4 + x6 + x7, -(-x2 - x3 + x5 - x8));
+      }
+    }
+  // backward post-processing in x and z
+  for (int k = 0; k < nz2; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        cplx& v = CW(i, j, k);
+        double t1 = v.real(), t2 = v.imag();
+        v = cplx(t1 * c.sbx[i] - t2 * c.sax[i], t2 * c.sbx[i] + t1 * c.sax[i]);
+        if (i + 1 > nx / 2 + 1) v = -v;
+        t1 = v.real(); t2 = v.imag();
+        v = cplx(t1 * c.sbz[k] - t2 * c.saz[k], t2 * c.sbz[k] + t1 * c.saz[k]);
+      }
+#pragma omp parallel
+  {
+    std::vector<cplx> line, work;
+#pragma omp for collapse(2)
+    for (int k = 0; k < nz2; ++k)
+      for (int j = 0; j < ny; ++j) {
+        line.resize(nx);
+        for (int i = 0; i < nx; ++i) line[i] = CW(i, j, k);
+        fft1d(line.data(), nx, +1, work);
+        for (int i = 0; i < nx; ++i) CW(i, j, k) = line[i];
+      }
+#pragma omp for collapse(2)
+    for (int k = 0; k < nz2; ++k)
+      for (int i = 0; i < nx; ++i) {
+        line.resize(ny);
+        for (int j = 0; j < ny; ++j) line[j] = CW(i, j, k);
+        fft1d(line.data(), ny, +1, work);
+        for (int j = 0; j < ny; ++j) CW(i, j, k) = line[j];
+      }
+#pragma omp for collapse(2)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        line.assign(nz, cplx(0, 0));
+        for (int k = 0; k < nz2; ++k) line[k] = CW(i, j, k);
+        for (int k = nz2; k < nz; ++k) line[k] = std::conj(CW(i, j, nz - k));
+        line[0] = cplx(line[0].real(), 0.0);
+        if (nz % 2 == 0) line[nz / 2] = cplx(line[nz / 2].real(), 0.0);
+        fft1d(line.data(), nz, +1, work);
+        for (int k = 0; k < nz; ++k) rhs[idx3(i, j, k, nx, ny)] = line[k].real();
+      }
+  }
+  // inverse reorder (src/poisson.f90:995-1006)
+  {
+    vec t(rhs, rhs + N);
+    for (int k = 0; k < nz; ++k)
+      for (int i = 0; i < nx; ++i)
+        for (int j = 1; j <= ny / 2; ++j) {
+          rhs[idx3(i, 2 * j - 2, k, nx, ny)] = t[idx3(i, j - 1, k, nx, ny)];
+          rhs[idx3(i, 2 * j - 1, k, nx, ny)] = t[idx3(i, ny - j, k, nx, ny)];
+        }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Incompressible step for the plain periodic case
 // ---------------------------------------------------------------------------
 struct Fields {
@@ -980,7 +1429,7 @@ static void momentum_rhs(const OxCtx& c, const vec& ux, const vec& uy, const vec
   // Y
   vec td2(N), te2(N), tf2(N), tg2(N), th2(N), ti2(N);
   for (size_t m = 0; m < N; ++m) { td2[m] = ux[m] * uy[m]; te2[m] = uy[m] * uy[m]; tf2[m] = uz[m] * uy[m]; }
-  pp = c.ppy.empty() ? nullptr : nullptr;  // istret=0 in the periodic configurations
+  pp = (c.istret != 0) ? c.ppy.data() : nullptr;  // dery multiplies by ppy when istret != 0
   apply3d(c, 1, OP_DER1, 0, td2.data(), tg2.data(), dims, pp);
   apply3d(c, 1, OP_DER1, 1, te2.data(), th2.data(), dims, pp);
   apply3d(c, 1, OP_DER1, 0, tf2.data(), ti2.data(), dims, pp);
@@ -1024,6 +1473,23 @@ static void momentum_rhs(const OxCtx& c, const vec& ux, const vec& uy, const vec
   apply3d(c, 1, OP_DER2, 1, ux.data(), td2.data(), dims, nullptr);
   apply3d(c, 1, OP_DER2, 0, uy.data(), te2.data(), dims, nullptr);
   apply3d(c, 1, OP_DER2, 1, uz.data(), tf2.data(), dims, nullptr);
+  if (c.istret != 0) {
+    // stretched mesh: d2/dy2 = deryy*pp2y - pp4y*dery (src/transeq.f90:335-370)
+    vec tj(N);
+    const vec* us[3] = {&ux, &uy, &uz};
+    vec* ts[3] = {&td2, &te2, &tf2};
+    const int par[3] = {1, 0, 1};
+    for (int q = 0; q < 3; ++q) {
+      apply3d(c, 1, OP_DER1, par[q], us[q]->data(), tj.data(), dims, c.ppy.data());
+      vec& t = *ts[q];
+      for (int k = 0; k < c.nz; ++k)
+        for (int j = 0; j < c.ny; ++j)
+          for (int i = 0; i < c.nx; ++i) {
+            const size_t m = idx3(i, j, k, c.nx, c.ny);
+            t[m] = t[m] * c.pp2y[j] - c.pp4y[j] * tj[m];
+          }
+    }
+  }
   vec ta2(N), tb2(N), tc2(N);
   for (size_t m = 0; m < N; ++m) {
     ta2[m] = xnu * td2[m] + tg2[m];
@@ -1046,7 +1512,8 @@ static void momentum_rhs(const OxCtx& c, const vec& ux, const vec& uy, const vec
   }
 }
 
-// divergence (nlock=1, periodic, no IBM): src/navier.f90:257-372.
+// divergence (nlock=1, no IBM): src/navier.f90:257-372; deryvp takes ppyi
+// on a stretched mesh.
 static void divergence(const OxCtx& c, const vec& ux, const vec& uy, const vec& uz, vec& pp3) {
   const size_t N = ux.size();
   const int dims[3] = {c.nx, c.ny, c.nz};
@@ -1058,7 +1525,7 @@ static void divergence(const OxCtx& c, const vec& ux, const vec& uy, const vec& 
   const int d2[3] = {nxm, c.ny, c.nz};
   vec upi2((size_t)nxm * nym * c.nz), duydypi2(upi2.size());
   apply3d(c, 1, OP_IVP, 1, pp1.data(), upi2.data(), d2, nullptr);
-  apply3d(c, 1, OP_DVP, 0, pgy1.data(), duydypi2.data(), d2, nullptr);
+  apply3d(c, 1, OP_DVP, 0, pgy1.data(), duydypi2.data(), d2, c.istret != 0 ? c.ppyi.data() : nullptr);
   for (size_t m = 0; m < upi2.size(); ++m) duydypi2[m] = duydypi2[m] + upi2[m];
   apply3d(c, 1, OP_IVP, 1, pgz1.data(), upi2.data(), d2, nullptr);
   const int d3[3] = {nxm, nym, c.nz};
@@ -1071,7 +1538,8 @@ static void divergence(const OxCtx& c, const vec& ux, const vec& uy, const vec& 
   (void)N;
 }
 
-// gradp: src/navier.f90:386-499 (periodic: no wall-gradient storage needed).
+// gradp: src/navier.f90:386-432; derypv takes ppy on a stretched mesh.  The
+// wall-gradient storage of src/navier.f90:434-499 is done by the caller.
 static void gradp(const OxCtx& c, const vec& pp3, vec& px, vec& py, vec& pz) {
   const int nxm = c.ax[0].nm, nym = c.ax[1].nm, nzm = c.ax[2].nm;
   const int d3[3] = {nxm, nym, nzm};
@@ -1081,7 +1549,7 @@ static void gradp(const OxCtx& c, const vec& pp3, vec& px, vec& py, vec& pz) {
   const int d2[3] = {nxm, nym, c.nz};
   vec ppi2((size_t)nxm * c.ny * c.nz), pgy2(ppi2.size()), pgzi2(ppi2.size());
   apply3d(c, 1, OP_IPV, 1, ppi3.data(), ppi2.data(), d2, nullptr);
-  apply3d(c, 1, OP_DPV, 1, ppi3.data(), pgy2.data(), d2, nullptr);
+  apply3d(c, 1, OP_DPV, 1, ppi3.data(), pgy2.data(), d2, c.istret != 0 ? c.ppy.data() : nullptr);
   apply3d(c, 1, OP_IPV, 1, pgz3.data(), pgzi2.data(), d2, nullptr);
   const int d1[3] = {nxm, c.ny, c.nz};
   apply3d(c, 0, OP_DPV, 1, ppi2.data(), px.data(), d1, nullptr);
@@ -1094,8 +1562,8 @@ static void gradp(const OxCtx& c, const vec& pp3, vec& px, vec& py, vec& pz) {
 // ---------------------------------------------------------------------------
 extern "C" {
 
-// ivals: nx,ny,nz, nclx1,nclxn, ncly1,nclyn, nclz1,nclzn, ifirstder,isecondder,ipinter
-// dvals: xlx,yly,zlz, filter_alpha, nu0nu, cnu
+// ivals: nx,ny,nz, nclx1,nclxn, ncly1,nclyn, nclz1,nclzn, ifirstder,isecondder,ipinter, istret
+// dvals: xlx,yly,zlz, filter_alpha, nu0nu, cnu, beta
 void* ox_create(const int* iv, const double* dv) {
   OxCtx* c = new OxCtx();
   c->nx = iv[0]; c->ny = iv[1]; c->nz = iv[2];
@@ -1105,6 +1573,18 @@ void* ox_create(const int* iv, const double* dv) {
   setup_axis(c->ax[0], c->nx, c->xlx, iv[3], iv[4], c->opts);
   setup_axis(c->ax[1], c->ny, c->yly, iv[5], iv[6], c->opts);
   setup_axis(c->ax[2], c->nz, c->zlz, iv[7], iv[8], c->opts);
+  c->istret = iv[12];
+  c->beta = dv[6];
+  stretching_setup(*c);
+  if (c->ax[0].periodic && !c->ax[1].periodic && c->ax[2].periodic) {
+    vec tmp;
+    waves_axis(c->ax[0], c->kx2, c->trx10);
+    waves_axis(c->ax[2], c->kz2, c->trz10);
+    waves_y010(*c, c->yky10, c->yk210, c->eys10, c->try10);
+    abxyz_axis(c->nx, c->sax, c->sbx);
+    abxyz_half(c->ax[1].nm, c->say, c->sby);
+    abxyz_axis(c->nz, c->saz, c->sbz);
+  }
   if (c->ax[0].periodic && c->ax[1].periodic && c->ax[2].periodic) {
     waves_axis(c->ax[0], c->kx2, c->tx);
     waves_axis(c->ax[1], c->ky2, c->ty);
@@ -1170,9 +1650,27 @@ int ox_scalars(void* h, int axis, double* out) {
 
 int ox_poisson(void* h, double* rhs) {
   const OxCtx* c = (const OxCtx*)h;
-  if (!(c->ax[0].periodic && c->ax[1].periodic && c->ax[2].periodic)) return -2;
-  poisson_000(*c, rhs);
-  return 0;
+  if (c->ax[0].periodic && c->ax[1].periodic && c->ax[2].periodic) {
+    poisson_000(*c, rhs);
+    return 0;
+  }
+  if (c->ax[0].periodic && !c->ax[1].periodic && c->ax[2].periodic) {
+    if (c->istret == 3) return -2;
+    poisson_010(*c, rhs);
+    return 0;
+  }
+  return -2;
+}
+
+// Stretching metrics: which = 0..7 -> yp, ypi, ppy, pp2y, pp4y, ppyi, pp2yi,
+// pp4yi; 8 -> {alpha}.
+int ox_stretching(void* h, int which, double* out) {
+  const OxCtx* c = (const OxCtx*)h;
+  const vec* tab[] = {&c->yp, &c->ypi, &c->ppy, &c->pp2y, &c->pp4y, &c->ppyi, &c->pp2yi, &c->pp4yi};
+  if (which == 8) { out[0] = c->alpha; return 1; }
+  if (which < 0 || which > 7) return -1;
+  std::memcpy(out, tab[which]->data(), tab[which]->size() * sizeof(double));
+  return (int)tab[which]->size();
 }
 
 int ox_divergence(void* h, const double* ux, const double* uy, const double* uz, double* pp3) {
@@ -1339,6 +1837,134 @@ int ox_run(void* h, double* ux_, double* uy_, double* uz_, int nsteps, double dt
   std::memcpy(uy_, uy.data(), N * sizeof(double));
   std::memcpy(uz_, uz.data(), N * sizeof(double));
   return row;
+}
+
+// Channel flow time loop (src/xcompact3d.f90:29-102 with the channel case):
+// per sub-step boundary_conditions -> channel_cfr (src/Case-Channel.f90:221-264,
+// constant flow rate 2/3), momentum_rhs_eq + momentum_forcing_channel
+// (src/Case-Channel.f90:392-421, rotation while itime < spinup_time), intt,
+// pre_correc's no-slip wall values (src/navier.f90:614-700), divergence,
+// poisson_010, gradp with the wall pressure-gradient storage
+// (src/navier.f90:456-477) and cor_vel.  Walls at y = 0 and y = Ly
+// (ncly1 = nclyn = 2) with zero wall velocity; x and z periodic.
+// ub_trace[s] receives the bulk velocity measured by channel_cfr at each
+// sub-step (before its correction).
+int ox_run_channel(void* h, double* ux_, double* uy_, double* uz_, int nsteps, double dt, double xnu, int itimescheme,
+                   double wrotation, int spinup_time, double* ub_trace, double* divmax) {
+  const OxCtx* c = (const OxCtx*)h;
+  if (!(c->ax[0].periodic && !c->ax[1].periodic && c->ax[2].periodic)) return -2;
+  if (c->ax[1].ncl1 != 2 || c->ax[1].ncln != 2) return -2;
+  const int nx = c->nx, ny = c->ny, nz = c->nz;
+  const size_t N = (size_t)nx * ny * nz;
+  vec ux(ux_, ux_ + N), uy(uy_, uy_ + N), uz(uz_, uz_ + N);
+  const int ntime = (itimescheme == 3) ? 3 : 2;
+  std::vector<vec> dux(ntime, vec(N, 0.0)), duy(ntime, vec(N, 0.0)), duz(ntime, vec(N, 0.0));
+  double adt[3] = {0, 0, 0}, bdt[3] = {0, 0, 0}, cdt[3] = {0, 0, 0}, gdt[3] = {0, 0, 0};
+  int nsub = 1;
+  if (itimescheme == 3) {
+    adt[0] = (23.0 / 12.0) * dt; bdt[0] = -(16.0 / 12.0) * dt; cdt[0] = (5.0 / 12.0) * dt;
+    gdt[0] = adt[0] + bdt[0] + cdt[0];
+  } else if (itimescheme == 5) {
+    nsub = 3;
+    adt[0] = (8.0 / 15.0) * dt; bdt[0] = 0; gdt[0] = adt[0];
+    adt[1] = (5.0 / 12.0) * dt; bdt[1] = (-17.0 / 60.0) * dt; gdt[1] = adt[1] + bdt[1];
+    adt[2] = (3.0 / 4.0) * dt; bdt[2] = (-5.0 / 12.0) * dt; gdt[2] = adt[2] + bdt[2];
+  } else {
+    return -3;
+  }
+  // wall pressure gradients dpdxy1, dpdzy1 (j = 1) and dpdxyn, dpdzyn (j = ny)
+  vec dpdxy1((size_t)nx * nz, 0.0), dpdzy1(dpdxy1.size(), 0.0), dpdxyn(dpdxy1.size(), 0.0),
+      dpdzyn(dpdxy1.size(), 0.0);
+  vec pp3, px(N), py(N), pz(N);
+  const double dy = c->ax[1].d;
+  const double coeff = dy / (c->yly * (double)(nx * nz));
+  int s = 0;
+  for (int itime = 1; itime <= nsteps; ++itime) {
+    for (int itr = 1; itr <= nsub; ++itr) {
+      // channel_cfr
+      double ub = 0.0;
+      for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+          for (int i = 0; i < nx; ++i) ub = ub + ux[idx3(i, j, k, nx, ny)] / c->ppy[j];
+      ub = ub * coeff;
+      const double can = -(2.0 / 3.0 - ub);
+      for (size_t m = 0; m < N; ++m) ux[m] = ux[m] - can;
+      if (ub_trace) ub_trace[s] = ub;
+      ++s;
+      momentum_rhs(*c, ux, uy, uz, xnu, dux[0], duy[0], duz[0]);
+      if (itime < spinup_time) {
+        for (size_t m = 0; m < N; ++m) {
+          dux[0][m] = dux[0][m] - wrotation * uy[m];
+          duy[0][m] = duy[0][m] + wrotation * ux[m];
+        }
+      }
+      vec* vars[3] = {&ux, &uy, &uz};
+      std::vector<vec>* dvs[3] = {&dux, &duy, &duz};
+      for (int q = 0; q < 3; ++q) {
+        vec& v = *vars[q];
+        std::vector<vec>& d = *dvs[q];
+        if (itimescheme == 3) {
+          if (itime == 1) {
+            for (size_t m = 0; m < N; ++m) v[m] = dt * d[0][m] + v[m];
+          } else if (itime == 2) {
+            for (size_t m = 0; m < N; ++m) v[m] = 1.5 * dt * d[0][m] - 0.5 * dt * d[1][m] + v[m];
+            d[2] = d[1];
+          } else {
+            for (size_t m = 0; m < N; ++m)
+              v[m] = adt[0] * d[0][m] + bdt[0] * d[1][m] + cdt[0] * d[2][m] + v[m];
+            d[2] = d[1];
+          }
+          d[1] = d[0];
+        } else {
+          if (itr == 1) {
+            for (size_t m = 0; m < N; ++m) v[m] = gdt[0] * d[0][m] + v[m];
+          } else {
+            for (size_t m = 0; m < N; ++m) v[m] = adt[itr - 1] * d[0][m] + bdt[itr - 1] * d[1][m] + v[m];
+          }
+          d[1] = d[0];
+        }
+      }
+      // pre_correc: no-slip walls with the stored tangential pressure gradient
+      const double g = gdt[itr - 1];
+      for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nx; ++i) {
+          const size_t w = (size_t)i + (size_t)nx * k;
+          dpdxy1[w] = dpdxy1[w] * g;
+          dpdzy1[w] = dpdzy1[w] * g;
+          dpdxyn[w] = dpdxyn[w] * g;
+          dpdzyn[w] = dpdzyn[w] * g;
+          ux[idx3(i, 0, k, nx, ny)] = 0.0 + dpdxy1[w];
+          uy[idx3(i, 0, k, nx, ny)] = 0.0;
+          uz[idx3(i, 0, k, nx, ny)] = 0.0 + dpdzy1[w];
+          ux[idx3(i, ny - 1, k, nx, ny)] = 0.0 + dpdxyn[w];
+          uy[idx3(i, ny - 1, k, nx, ny)] = 0.0;
+          uz[idx3(i, ny - 1, k, nx, ny)] = 0.0 + dpdzyn[w];
+        }
+      divergence(*c, ux, uy, uz, pp3);
+      poisson_010(*c, pp3.data());
+      gradp(*c, pp3, px, py, pz);
+      for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nx; ++i) {
+          const size_t w = (size_t)i + (size_t)nx * k;
+          dpdxy1[w] = px[idx3(i, 0, k, nx, ny)] / g;
+          dpdzy1[w] = pz[idx3(i, 0, k, nx, ny)] / g;
+          dpdxyn[w] = px[idx3(i, ny - 1, k, nx, ny)] / g;
+          dpdzyn[w] = pz[idx3(i, ny - 1, k, nx, ny)] / g;
+        }
+      for (size_t m = 0; m < N; ++m) { ux[m] = ux[m] - px[m]; uy[m] = uy[m] - py[m]; uz[m] = uz[m] - pz[m]; }
+    }
+  }
+  if (divmax) {
+    vec p;
+    divergence(*c, ux, uy, uz, p);
+    double dmax = 0;
+    for (double v : p) dmax = std::max(dmax, std::fabs(v));
+    *divmax = dmax;
+  }
+  std::memcpy(ux_, ux.data(), N * sizeof(double));
+  std::memcpy(uy_, uy.data(), N * sizeof(double));
+  std::memcpy(uz_, uz.data(), N * sizeof(double));
+  return s;
 }
 
 }  // extern "C"
