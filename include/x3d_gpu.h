@@ -55,7 +55,8 @@ typedef struct {
   int nx, ny, nz;
   double xlx, yly, zlz;
   int nclx1, nclxn, ncly1, nclyn, nclz1, nclzn;
-  int istret;  /* mesh stretching in y; only 0 is implemented */
+  int istret;  /* mesh stretching in y (src/stretching.f90): 0 none, 1 centre,
+                  2 both walls, 3 bottom wall; needs a non-periodic y */
   double beta;
 } x3d_grid;
 
@@ -104,7 +105,10 @@ int x3d_get_coeffs(const x3d_ctx* ctx, int axis, int which, double* out, int cap
  * DERIVATIVE_X / _Y / _YY / _Z interfaces, src/module_param.f90:135-170;
  * implementations src/derive.f90:7-3792 (derx_00 ... derzz_22, bound by BC in
  * src/schemes.f90:30-64).  lind is used by the reference only for IBM and is
- * ignored.  ppy (dery only) is applied when the grid is stretched. */
+ * ignored.  ppy (dery only) is applied when the grid is stretched (istret !=
+ * 0, src/derive.f90:409-418): the result is multiplied by the context's ppy;
+ * a ppy passed by the caller must equal it bit for bit (else X3D_ERR_COEF),
+ * NULL takes the context's.  deryvp takes ppyi and derypv ppy the same way. */
 int x3d_derx(x3d_ctx* ctx, double* tx, const double* ux, double* rx, double* sx, const double* ffx,
              const double* fsx, const double* fwx, int nx, int ny, int nz, int npaire, double lind,
              void* stream);
@@ -206,11 +210,17 @@ int x3d_fily_f32(x3d_ctx* ctx, float* ty, const float* uy, int nx, int ny, int n
 int x3d_filz_f32(x3d_ctx* ctx, float* tz, const float* uz, int nx, int ny, int nz, int npaire, void* stream);
 
 /* --- Poisson solve ------------------------------------------------------------
- * poisson(rhs) procedure pointer, src/poisson.f90:57-62; all-periodic solver
- * poisson_000, src/poisson.f90:298-410.  rhs (nxm,nym,nzm) in device memory is
- * overwritten by the solution.  precision: 0 = FP64 FFT, 1 = FP32 FFT,
- * 2 = double-float FFT (each real carried as a hi+lo pair of binary32,
- * ~48-bit significand, computed on the FP32 pipes). */
+ * poisson(rhs) procedure pointer, src/poisson.f90:57-62, chosen from the
+ * boundary conditions as decomp_2d_poisson_init does (src/poisson.f90:97-107):
+ *   all periodic                 -> poisson_000, src/poisson.f90:298-410;
+ *   x, z periodic, y walls       -> poisson_010, src/poisson.f90:665-1013
+ *     (cosine transform in y; on a stretched mesh, istret 1 or 2, the two
+ *     pentadiagonal systems of matrice_refinement, src/poisson.f90:1814-2113,
+ *     solved as inversion5_v1, src/tools.f90:1225-1362).
+ * rhs (nxm,nym,nzm) in device memory is overwritten by the solution.
+ * precision (poisson_000 only): 0 = FP64 FFT, 1 = FP32 FFT, 2 = double-float
+ * FFT (each real carried as a hi+lo pair of binary32, ~48-bit significand,
+ * computed on the FP32 pipes).  poisson_010 runs in FP64. */
 int x3d_poisson(x3d_ctx* ctx, double* rhs, void* stream);
 int x3d_poisson_ex(x3d_ctx* ctx, double* rhs, int precision, void* stream);
 
@@ -232,6 +242,13 @@ int x3d_poisson_ex(x3d_ctx* ctx, double* rhs, int precision, void* stream);
 #define X3D_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
 int x3d_poisson_noalloc(x3d_ctx* ctx, double* rhs, void* stream);
 
+/* Host copy of the y-mesh metrics computed at context creation (module
+ * variables yp, ypi, ppy, pp2y, pp4y, ppyi, pp2yi, pp4yi of
+ * src/variables.f90:1294-1336 / src/stretching.f90:92-270): which = 0..7 in
+ * that order (ny values each), 8 = the mapping constant alpha.  Returns the
+ * number of values written. */
+int x3d_get_stretching(const x3d_ctx* ctx, int which, double* out, int capacity);
+
 /* --- 2DECOMP transposes ------------------------------------------------------
  * transpose_x_to_y / y_to_z / z_to_y / y_to_x of 2DECOMP&FFT.  On one GPU the
  * X-, Y- and Z-pencils are the same (nx,ny,nz) array, so each is a device copy
@@ -250,11 +267,14 @@ int x3d_gradp(x3d_ctx* ctx, double* px, double* py, double* pz, const double* pp
 int x3d_cor_vel(x3d_ctx* ctx, double* ux, double* uy, double* uz, const double* px, const double* py,
                 const double* pz, void* stream);
 
-/* --- incompressible solver (the time loop body of src/xcompact3d.f90:29-102)
- * for the plain periodic case: calculate_transeq_rhs (src/transeq.f90:20-591),
- * int_time (src/time_integrators.f90), solve_poisson + cor_vel
+/* --- incompressible solver (the time loop body of src/xcompact3d.f90:29-102):
+ * calculate_transeq_rhs (src/transeq.f90:20-591), int_time
+ * (src/time_integrators.f90), pre_correc, solve_poisson + cor_vel
  * (src/navier.f90).  The solver owns u, v, w, the time-integrator history and
  * the work fields, all resident in device memory.
+ * Geometries: triply periodic (poisson_000), or the channel: x and z
+ * periodic with no-slip walls at both y ends (ncly1 = nclyn = 2, optionally a
+ * stretched y mesh, poisson_010), FP64 only.
  * precision: X3D_PREC_FP64 computes everything in binary64;
  * X3D_PREC_MIXED runs derivatives, convective/viscous terms and the staggered
  * operators in binary32, keeps the velocity, the time-integrator history and
@@ -283,6 +303,17 @@ int x3d_solver_tgv_stats(x3d_solver* s, double* out, void* stream);
 int x3d_solver_divmax(x3d_solver* s, double* out, void* stream);
 /* Number of kernels this solver launches per time step. */
 int x3d_solver_launches_per_step(x3d_solver* s);
+/* Channel case (itype = channel, src/Case-Channel.f90): before every sub-step
+ * channel_cfr (src/Case-Channel.f90:221-264) shifts u so that the bulk
+ * velocity is target_ub (the reference uses 2/3); while the step index is
+ * below spinup_time the rotation forcing of momentum_forcing_channel
+ * (src/Case-Channel.f90:392-421) with speed wrotation is added.  The no-slip
+ * wall values of pre_correc and the wall pressure gradients of gradp are
+ * always applied in the channel geometry.  X3D_ERR_BC on a periodic solver. */
+int x3d_solver_set_channel(x3d_solver* s, double target_ub, double wrotation, int spinup_time);
+/* Bulk velocity measured by channel_cfr (before its correction) at each
+ * sub-step of the last step; returns the number of values.  Synchronises. */
+int x3d_solver_bulk_velocity(x3d_solver* s, double* out, int capacity);
 
 #ifdef __cplusplus
 }

@@ -119,6 +119,9 @@ def load():
         lib.x3d_solver_tgv_stats.argtypes = [P, P, P]
         lib.x3d_solver_divmax.argtypes = [P, P, P]
         lib.x3d_solver_launches_per_step.argtypes = [P]
+        lib.x3d_solver_set_channel.argtypes = [P, D, D, I]
+        lib.x3d_solver_bulk_velocity.argtypes = [P, P, I]
+        lib.x3d_get_stretching.argtypes = [P, I, P, I]
         _lib = lib
         return lib
 

@@ -19,6 +19,8 @@ Ctx::~Ctx() {
     if (d_k2df[a]) cudaFree(d_k2df[a]);
     if (d_trdf[a]) cudaFree(d_trdf[a]);
   }
+  if (st.d_ppy) cudaFree(st.d_ppy);
+  if (d_p010) cudaFree(d_p010);
   if (d_twid) cudaFree(d_twid);
   if (d_twid32) cudaFree(d_twid32);
   if (d_twid_df) cudaFree(d_twid_df);
@@ -60,6 +62,26 @@ int get_plan(Ctx* c, int axis, int kind, int npaire, int coefset, OpPlan** out) 
   return X3D_OK;
 }
 
+// Device copies of the stretching metrics: ppy | pp2y | pp4y | ppyi.
+int stretch_device(Ctx* c, const double** out) {
+  if (!c->st.d_ppy) {
+    const int ny = c->grid.ny;
+    dvec h;
+    for (const dvec* v : {&c->st.ppy, &c->st.pp2y, &c->st.pp4y, &c->st.ppyi}) h.insert(h.end(), v->begin(), v->end());
+    double* d = nullptr;
+    if (cudaMalloc(&d, h.size() * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
+    cudaError_t e = cudaMemcpy(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(d);
+      return cuda_status(e);
+    }
+    c->st.d_ppy = d;
+    (void)ny;
+  }
+  *out = c->st.d_ppy;
+  return X3D_OK;
+}
+
 }  // namespace x3d
 
 using namespace x3d;
@@ -92,7 +114,8 @@ int resolve_set(Ctx* c, int axis, int kind, int npaire, const double* f, const d
 }
 
 template <typename T>
-int run_op(x3d_ctx* h, int axis, int kind, int npaire, int coefset, T* t, const T* u, const int* dims, void* st) {
+int run_op(x3d_ctx* h, int axis, int kind, int npaire, int coefset, T* t, const T* u, const int* dims, void* st,
+           const T* pp = nullptr) {
   if (!h || !t || !u) return X3D_ERR_ARG;
   if (npaire != 0 && npaire != 1) return X3D_ERR_ARG;
   Ctx* c = C(h);
@@ -104,12 +127,28 @@ int run_op(x3d_ctx* h, int axis, int kind, int npaire, int coefset, T* t, const 
   OpPlan* p = nullptr;
   int rc = get_plan(c, axis, kind, npaire, coefset, &p);
   if (rc != X3D_OK) return rc;
-  return launch_line_op<T>(c, p, t, u, dims, nullptr, (cudaStream_t)st);
+  return launch_line_op<T>(c, p, t, u, dims, pp, (cudaStream_t)st);
+}
+
+// The y-metric a y operator multiplies by on a stretched mesh
+// (src/derive.f90:409-418 and likewise): `which` 0 = ppy, 3 = ppyi, applied
+// only when istret != 0.  A vector passed by the caller must equal the
+// context's bit for bit.
+int y_metric(Ctx* c, int which, const double* passed, const double** dev) {
+  *dev = nullptr;
+  if (c->st.istret == 0) return X3D_OK;
+  const dvec& v = (which == 0) ? c->st.ppy : c->st.ppyi;
+  if (passed && std::memcmp(passed, v.data(), v.size() * sizeof(double)) != 0) return X3D_ERR_COEF;
+  const double* d = nullptr;
+  int rc = stretch_device(c, &d);
+  if (rc != X3D_OK) return rc;
+  *dev = d + (size_t)which * c->grid.ny;
+  return X3D_OK;
 }
 
 // Operators along the grid axis with full (n) extents.
 int colloc(x3d_ctx* h, int axis, int kind, double* t, const double* u, const double* f, const double* s,
-           const double* w, int nx, int ny, int nz, int npaire, void* st) {
+           const double* w, int nx, int ny, int nz, int npaire, void* st, const double* pp = nullptr) {
   if (!h) return X3D_ERR_ARG;
   Ctx* c = C(h);
   if (nx != c->grid.nx || ny != c->grid.ny || nz != c->grid.nz) return X3D_ERR_SHAPE;
@@ -118,7 +157,7 @@ int colloc(x3d_ctx* h, int axis, int kind, double* t, const double* u, const dou
   int rc = resolve_set(c, axis, kind, npaire, f, s, w, &cs);
   if (rc != X3D_OK) return rc;
   const int dims[3] = {nx, ny, nz};
-  return run_op<double>(h, axis, kind, npaire, cs, t, u, dims, st);
+  return run_op<double>(h, axis, kind, npaire, cs, t, u, dims, st, pp);
 }
 
 int colloc32(x3d_ctx* h, int axis, int kind, float* t, const float* u, int nx, int ny, int nz, int npaire,
@@ -133,7 +172,7 @@ int colloc32(x3d_ctx* h, int axis, int kind, float* t, const float* u, int nx, i
 // Staggered operator: dims_in are the input extents.
 int stag(x3d_ctx* h, int axis, int kind, double* t, const double* u, const double* f1, const double* s1,
          const double* w1, const double* f2, const double* s2, const double* w2, const int* dims_in, int npaire,
-         void* st) {
+         void* st, const double* pp = nullptr) {
   if (!h) return X3D_ERR_ARG;
   Ctx* c = C(h);
   if (npaire != 0 && npaire != 1) return X3D_ERR_ARG;
@@ -156,7 +195,7 @@ int stag(x3d_ctx* h, int axis, int kind, double* t, const double* u, const doubl
       if (rc != X3D_OK) return rc;
     }
   }
-  return run_op<double>(h, axis, kind, npaire, cs, t, u, dims_in, st);
+  return run_op<double>(h, axis, kind, npaire, cs, t, u, dims_in, st, pp);
 }
 
 }  // namespace
@@ -187,7 +226,6 @@ const char* x3d_strerror(int s) {
 int x3d_ctx_create(const x3d_grid* g, const x3d_numopts* o, x3d_ctx** out) {
   if (!g || !o || !out) return X3D_ERR_ARG;
   *out = nullptr;
-  if (g->istret != 0) return X3D_ERR_UNSUPPORTED;
   if (g->nx < 8 || g->ny < 8 || g->nz < 8) return X3D_ERR_SHAPE;
   if (!(g->xlx > 0) || !(g->yly > 0) || !(g->zlz > 0)) return X3D_ERR_ARG;
   std::unique_ptr<Ctx> c(new Ctx());
@@ -204,6 +242,7 @@ int x3d_ctx_create(const x3d_grid* g, const x3d_numopts* o, x3d_ctx** out) {
   int rc = build_axis(c->ax[0], g->nx, g->xlx, g->nclx1, g->nclxn, *o);
   if (rc == X3D_OK) rc = build_axis(c->ax[1], g->ny, g->yly, g->ncly1, g->nclyn, *o);
   if (rc == X3D_OK) rc = build_axis(c->ax[2], g->nz, g->zlz, g->nclz1, g->nclzn, *o);
+  if (rc == X3D_OK) rc = build_stretch(*g, c->ax[1], c->st);
   if (rc != X3D_OK) return rc;
   *out = reinterpret_cast<x3d_ctx*>(c.release());
   return X3D_OK;
@@ -247,10 +286,12 @@ int x3d_derx(x3d_ctx* h, double* tx, const double* ux, double*, double*, const d
   return colloc(h, 0, K_DER1, tx, ux, ffx, fsx, fwx, nx, ny, nz, npaire, st);
 }
 int x3d_dery(x3d_ctx* h, double* ty, const double* uy, double*, double*, const double* ffy, const double* fsy,
-             const double* fwy, const double*, int nx, int ny, int nz, int npaire, double, void* st) {
-  // ppy is applied by the reference only when istret != 0; stretching is
-  // rejected at context creation, so it is never needed here.
-  return colloc(h, 1, K_DER1, ty, uy, ffy, fsy, fwy, nx, ny, nz, npaire, st);
+             const double* fwy, const double* ppy, int nx, int ny, int nz, int npaire, double, void* st) {
+  if (!h) return X3D_ERR_ARG;
+  const double* pp = nullptr;
+  int rc = y_metric(C(h), 0, ppy, &pp);
+  if (rc != X3D_OK) return rc;
+  return colloc(h, 1, K_DER1, ty, uy, ffy, fsy, fwy, nx, ny, nz, npaire, st, pp);
 }
 int x3d_derz(x3d_ctx* h, double* tz, const double* uz, double*, double*, const double* ffz, const double* fsz,
              const double* fwz, int nx, int ny, int nz, int npaire, double, void* st) {
@@ -343,10 +384,13 @@ int x3d_interyvp(x3d_ctx* h, double* ty, const double* uy, double*, double*, con
   return stag(h, 1, K_IVP, ty, uy, cify6, cisy6, ciwy6, nullptr, nullptr, nullptr, d, npaire, st);
 }
 int x3d_deryvp(x3d_ctx* h, double* ty, const double* uy, double*, double*, const double* cfy6, const double* csy6,
-               const double* cwy6, const double*, int nx, int ny, int nym, int nz, int npaire, void* st) {
+               const double* cwy6, const double* ppyi, int nx, int ny, int nym, int nz, int npaire, void* st) {
   if (!h || nym != C(h)->ax[1].nm) return h ? X3D_ERR_SHAPE : X3D_ERR_ARG;
+  const double* pp = nullptr;
+  int rc = y_metric(C(h), 3, ppyi, &pp);
+  if (rc != X3D_OK) return rc;
   const int d[3] = {nx, ny, nz};
-  return stag(h, 1, K_DVP, ty, uy, cfy6, csy6, cwy6, nullptr, nullptr, nullptr, d, npaire, st);
+  return stag(h, 1, K_DVP, ty, uy, cfy6, csy6, cwy6, nullptr, nullptr, nullptr, d, npaire, st, pp);
 }
 int x3d_interypv(x3d_ctx* h, double* ty, const double* uy, double*, double*, const double* cifi6y,
                  const double* cisi6y, const double* ciwi6y, const double* cify6, const double* cisy6,
@@ -357,10 +401,13 @@ int x3d_interypv(x3d_ctx* h, double* ty, const double* uy, double*, double*, con
 }
 int x3d_derypv(x3d_ctx* h, double* ty, const double* uy, double*, double*, const double* cfi6y,
                const double* csi6y, const double* cwi6y, const double* cfy6, const double* csy6,
-               const double* cwy6, const double*, int nx, int nym, int ny, int nz, int npaire, void* st) {
+               const double* cwy6, const double* ppy, int nx, int nym, int ny, int nz, int npaire, void* st) {
   if (!h || nym != C(h)->ax[1].nm) return h ? X3D_ERR_SHAPE : X3D_ERR_ARG;
+  const double* pp = nullptr;
+  int rc = y_metric(C(h), 0, ppy, &pp);
+  if (rc != X3D_OK) return rc;
   const int d[3] = {nx, nym, nz};
-  return stag(h, 1, K_DPV, ty, uy, cfi6y, csi6y, cwi6y, cfy6, csy6, cwy6, d, npaire, st);
+  return stag(h, 1, K_DPV, ty, uy, cfi6y, csi6y, cwi6y, cfy6, csy6, cwy6, d, npaire, st, pp);
 }
 int x3d_derzvp(x3d_ctx* h, double* tz, const double* uz, double*, double*, const double* cfz6, const double* csz6,
                const double* cwz6, int nx, int ny, int nz, int nzm, int npaire, void* st) {
@@ -394,7 +441,9 @@ int x3d_interzpv(x3d_ctx* h, double* tz, const double* uz, double*, double*, con
 // ---- Poisson, transposes, projection pieces ---------------------------------
 int x3d_poisson(x3d_ctx* h, double* rhs, void* st) {
   if (!h || !rhs) return X3D_ERR_ARG;
-  return poisson_periodic(C(h), rhs, 0, (cudaStream_t)st);
+  Ctx* c = C(h);
+  if (c->ax[0].periodic && !c->ax[1].periodic && c->ax[2].periodic) return poisson_010(c, rhs, (cudaStream_t)st);
+  return poisson_periodic(c, rhs, 0, (cudaStream_t)st);
 }
 int x3d_poisson_noalloc(x3d_ctx* h, double* rhs, void* st) {
   if (!h || !rhs) return X3D_ERR_ARG;
@@ -402,7 +451,26 @@ int x3d_poisson_noalloc(x3d_ctx* h, double* rhs, void* st) {
 }
 int x3d_poisson_ex(x3d_ctx* h, double* rhs, int precision, void* st) {
   if (!h || !rhs) return X3D_ERR_ARG;
-  return poisson_periodic(C(h), rhs, precision, (cudaStream_t)st);
+  Ctx* c = C(h);
+  if (c->ax[0].periodic && !c->ax[1].periodic && c->ax[2].periodic)
+    return precision == 0 ? poisson_010(c, rhs, (cudaStream_t)st) : X3D_ERR_DTYPE;
+  return poisson_periodic(c, rhs, precision, (cudaStream_t)st);
+}
+
+int x3d_get_stretching(const x3d_ctx* h, int which, double* out, int capacity) {
+  if (!h || !out) return X3D_ERR_ARG;
+  const Stretch& st = reinterpret_cast<const Ctx*>(h)->st;
+  if (which == 8) {
+    if (capacity < 1) return X3D_ERR_ARG;
+    out[0] = st.alpha;
+    return 1;
+  }
+  const dvec* tab[] = {&st.yp, &st.ypi, &st.ppy, &st.pp2y, &st.pp4y, &st.ppyi, &st.pp2yi, &st.pp4yi};
+  if (which < 0 || which > 7) return X3D_ERR_ARG;
+  const dvec& v = *tab[which];
+  if ((int)v.size() > capacity) return X3D_ERR_ARG;
+  std::memcpy(out, v.data(), v.size() * sizeof(double));
+  return (int)v.size();
 }
 
 static int tcopy(x3d_ctx* h, const double* src, double* dst, long long n, void* st) {

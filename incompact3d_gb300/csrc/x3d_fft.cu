@@ -742,4 +742,320 @@ int poisson_periodic_noalloc(Ctx* c, double* rhs, cudaStream_t st) {
   return cuda_status(cudaGetLastError());
 }
 
+// ---------------------------------------------------------------------------
+// poisson_010: x and z periodic, y non-periodic (src/poisson.f90:665-1013).
+//
+// The reference reorders y (even points forward, odd points backward), takes
+// a 3-D FFT, turns the y-spectrum into a cosine spectrum with the half-sample
+// combination of modes j and ny-j (src/poisson.f90:764-785), solves in y
+// (division by kxyz, or on a stretched mesh the two pentadiagonal systems of
+// the odd and even modes, src/poisson.f90:834-880 with src/tools.f90:
+// 1225-1362) and undoes everything.  The x and z half-cell shift factors
+// cancel as in poisson_000, and the y reorder commutes with the x and z
+// transforms, so the GPU does:
+//   A  x real-to-complex;  B  z forward FFT;
+//   C  one kernel per batch of (kx, kz) lines: gather y in reordered order,
+//      forward FFT, cosine combination, solve, inverse combination, inverse
+//      FFT, scatter back in reordered order -- the y-spectrum stays in shared
+//      memory;
+//   D  z inverse FFT;  E  x complex-to-real.
+// The pentadiagonal coefficients are formed on the fly per line from 1-D
+// tables (matrice_refinement's formulas), one thread per (line, odd/even
+// system), and eliminated in the reference's order with its epsilon guards.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct P010 {
+  const double *kx2, *trx, *kz2, *trz;  // x (nx/2+1 used) and z (nz, mirrored) tables
+  const double *yk2, *ty, *yky, *say, *sby;  // y tables, nym entries
+  const double2 *twy_f, *twy_i;
+  double xa0, xa1, scale;
+  int istret, nx, nz, nym, nsolve;  // nsolve = threads of the solve phase (2 per line)
+};
+
+__device__ __forceinline__ double2 cosine_fwd(double2 v, double2 w, double ay, double by) {
+  const double x1 = v.x * by, x2 = v.x * ay, x3 = v.y * by, x4 = v.y * ay;
+  const double x5 = w.x * by, x6 = w.x * ay, x7 = w.y * by, x8 = w.y * ay;
+  return make_double2(0.5 * (x1 + x4 + x5 - x8), 0.5 * (-x2 + x3 + x6 + x7));
+}
+__device__ __forceinline__ double2 cosine_bwd(double2 v, double2 w, double ay, double by) {
+  const double x1 = v.x * by, x2 = v.x * ay, x3 = v.y * by, x4 = v.y * ay;
+  const double x5 = w.x * by, x6 = w.x * ay, x7 = w.y * by, x8 = w.y * ay;
+  return make_double2(x1 - x4 + x6 + x7, -(-x2 - x3 + x5 - x8));
+}
+
+// Pentadiagonal solve of one (kx, kz) line's odd (sys 0) or even (sys 1) y
+// modes, in place on e[2m + sys], m = 0..nh-1.  band: 5 diagonals x nh rows,
+// interleaved over the T solve threads (entry (q, m) at band[(q*nh + m)*T]).
+__device__ void penta_line(double2* e, double* band, int T, int nh, int sys, int kx, int kz, const P010& q) {
+  auto B = [&](int qq, int m) -> double& { return band[(size_t)(qq * nh + m) * T]; };
+  const double kx2 = q.kx2[kx], kz2 = q.kz2[kz], tx = q.trx[kx], tz = q.trz[kz];
+  const double tx2 = tx * tx, tz2 = tz * tz;
+  const double xa0 = q.xa0, xa1 = q.xa1;
+  const double xa0_2 = xa0 * xa0, xa1_2 = xa1 * xa1, xa01 = xa0 * xa1, xa0p1_2 = (xa0 + xa1) * (xa0 + xa1);
+  auto cw = [&](int m) { return tx * (q.yky[2 * m + sys] * tz); };
+  auto ty2 = [&](int m) { const double t = q.ty[2 * m + sys]; return t * t; };
+  // diagonals (matrice_refinement, src/poisson.f90:1925-2113)
+  for (int m = 0; m < nh; ++m) {
+    const double c0 = cw(m);
+    const double cm = m > 0 ? cw(m - 1) : 0.0, cp = m + 1 < nh ? cw(m + 1) : 0.0;
+    double a2c = xa0_2, nb = cm + cp;
+    if (m == 0) { nb = cp; if (sys == 1) a2c = xa0_2 - xa1_2; }
+    if (m == nh - 1) { nb = cm; if (sys == 1) a2c = xa0p1_2; }
+    B(2, m) = -(kx2 * ty2(m) * tz2 + kz2 * ty2(m) * tx2 + a2c * (c0 * c0) + xa1_2 * c0 * nb);
+    B(3, m) = (m + 1 < nh) ? xa01 * (cp * (c0 + cp)) : 0.0;
+    B(4, m) = (m + 2 < nh) ? xa1_2 * (-(cp * cw(m + 2))) : 0.0;
+    B(1, m) = (m > 0) ? xa01 * (cm * (c0 + cm)) : 0.0;
+    B(0, m) = (m > 1) ? xa1_2 * (-(cm * cw(m - 2))) : 0.0;
+  }
+  {
+    const double c0 = cw(0), c1 = cw(1);
+    if (sys == 0) {
+      B(3, 0) = 2.0 * xa01 * (c0 * c1 + c1 * c1);
+      B(4, 0) = 2.0 * B(4, 0);
+    } else {
+      B(3, 0) = (xa0 - xa1) * xa1 * (c0 * c1) + xa0 * xa1 * (c1 * c1);
+      B(1, 1) = xa0 * xa1 * (c1 * c0) + (xa0 + xa1) * xa1 * (c0 * c0);
+      const double ca = cw(nh - 2), cb = cw(nh - 1);
+      B(3, nh - 2) = xa0 * xa1 * ca * cb + (xa0 + xa1) * xa1 * (cb * cb);
+      B(1, nh - 1) = (xa0 + xa1) * xa1 * (cb * ca) + xa0 * xa1 * (ca * ca);
+    }
+    B(4, nh - 2) = 0.0;
+    if (sys == 0 && kx2 == 0.0 && kz2 == 0.0) {
+      B(2, 0) = 1.0; B(3, 0) = 0.0; B(4, 0) = 0.0;
+    }
+  }
+  // inversion5_v1: forward elimination
+  const double eps = 1.0e-16;
+  auto E = [&](int m) -> double2& { return e[2 * m + sys]; };
+  double tmp = 0.0;
+  for (int m = 0; m <= nh - 3; ++m)
+    for (int ii = 1; ii <= 2; ++ii) {
+      const int mi = m + ii;
+      const double piv = B(2, m);
+      if (piv != 0.0) tmp = B(2 - ii, mi) / piv;
+      const double2 em = E(m), emi = E(mi);
+      E(mi) = make_double2(emi.x - tmp * em.x, emi.y - tmp * em.y);
+      const int j0 = (ii == 1) ? 2 : 1;
+      for (int jc = j0; jc <= j0 + 1; ++jc) B(jc, mi) = B(jc, mi) - tmp * B(jc + ii, m);
+    }
+  {
+    const double p1 = B(2, nh - 2);
+    const double sr = (fabs(p1) > eps) ? B(1, nh - 1) / p1 : 0.0;
+    const double b1 = B(2, nh - 1) - sr * B(3, nh - 2);
+    const double2 en = E(nh - 1), en1 = E(nh - 2);
+    double2 t3 = make_double2(0.0, 0.0);
+    if (fabs(b1) > eps) {
+      const double t1 = sr / b1;
+      t3 = make_double2(en.x / b1 - t1 * en1.x, en.y / b1 - t1 * en1.y);
+    }
+    E(nh - 1) = t3;
+    const double r = (fabs(p1) > eps) ? 1.0 / p1 : 0.0;
+    const double a1 = B(3, nh - 2) * r;
+    E(nh - 2) = make_double2(en1.x * r - a1 * t3.x, en1.y * r - a1 * t3.y);
+  }
+  for (int i = nh - 3; i >= 0; --i) {
+    const double p = B(2, i);
+    const double r = (fabs(p) > eps) ? 1.0 / p : 0.0;
+    const double a1 = B(3, i) * r, b1 = B(4, i) * r;
+    const double2 e0 = E(i), e1 = E(i + 1), e2 = E(i + 2);
+    E(i) = make_double2(e0.x * r - a1 * e1.x - b1 * e2.x, e0.y * r - a1 * e1.y - b1 * e2.y);
+  }
+}
+
+// Pass C.  Lines: kx = blockIdx.x*lanes + l (stride 1), kz = blockIdx.y; the
+// y row stride is rs = nx/2+1, the kz plane stride bs = (nx/2+1)*nym.
+__global__ void __launch_bounds__(FFT_THREADS) k_p010_y(double2* __restrict__ data, long long rs, int na, int lanes,
+                                                        long long bs, P010 q) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = q.nym, nh = n / 2, ls = n + 1;
+  double2* buf = reinterpret_cast<double2*>(smem_raw);
+  double* band = reinterpret_cast<double*>(buf + (size_t)lanes * ls);
+  const int a0 = blockIdx.x * lanes;
+  const int nl = min(lanes, na - a0);
+  const int kz = blockIdx.y;
+  double2* base = data + (long long)kz * bs + a0;
+  // gather in the reordered y order (src/poisson.f90:688-698)
+  for (int e = threadIdx.x; e < lanes * n; e += FFT_THREADS) {
+    const int r = e / lanes, l = e - r * lanes;
+    const int src = (r < nh) ? 2 * r : 2 * n - 2 * r - 1;
+    if (l < nl) buf[l * ls + r] = base[src * rs + l];
+  }
+  __syncthreads();
+  smem_fft<-1, double>(buf, ls, n, nl, q.twy_f);
+  // cosine combination of modes j and n-j, with the 1/(nx nym nz) normalisation
+  for (int e = threadIdx.x; e < nl * nh; e += FFT_THREADS) {
+    const int l = e / nh, j = 1 + (e - l * nh), jp = n - j;
+    double2* line = buf + l * ls;
+    const double2 v = line[j], w = line[jp];
+    const double2 sv = make_double2(v.x * q.scale, v.y * q.scale), sw = make_double2(w.x * q.scale, w.y * q.scale);
+    line[j] = cosine_fwd(sv, sw, q.say[j], q.sby[j]);
+    if (jp != j) line[jp] = cosine_fwd(sw, sv, q.say[jp], q.sby[jp]);
+    if (j == 1) line[0] = make_double2(line[0].x * q.scale, line[0].y * q.scale);
+  }
+  __syncthreads();
+  if (q.istret == 0) {
+    for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
+      const int l = e / n, j = e - l * n;
+      const int kx = a0 + l;
+      const double pyz = __dmul_rn(q.ty[j], q.trz[kz]), pxz = __dmul_rn(q.trx[kx], q.trz[kz]),
+                   pxy = __dmul_rn(q.trx[kx], q.ty[j]);
+      const double kk = __dadd_rn(__dadd_rn(__dmul_rn(q.kx2[kx], __dmul_rn(pyz, pyz)), __dmul_rn(q.yk2[j], __dmul_rn(pxz, pxz))),
+                                  __dmul_rn(q.kz2[kz], __dmul_rn(pxy, pxy)));
+      double2& v = buf[l * ls + j];
+      if (fabs(kk) < 1.0e-16) v = make_double2(0.0, 0.0);
+      else v = make_double2(v.x / (-kk), v.y / (-kk));
+    }
+  } else if (threadIdx.x < 2 * nl) {
+    const int l = threadIdx.x >> 1, sys = threadIdx.x & 1;
+    penta_line(buf + l * ls, band + threadIdx.x, q.nsolve, nh, sys, a0 + l, kz, q);
+  }
+  __syncthreads();
+  // the (nx/2, nz/2) line is zeroed (src/poisson.f90:887-894)
+  if (kz == q.nz / 2)
+    for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
+      const int l = e / n, j = e - l * n;
+      if (a0 + l == q.nx / 2) buf[l * ls + j] = make_double2(0.0, 0.0);
+    }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nl * nh; e += FFT_THREADS) {
+    const int l = e / nh, j = 1 + (e - l * nh), jp = n - j;
+    double2* line = buf + l * ls;
+    const double2 v = line[j], w = line[jp];
+    line[j] = cosine_bwd(v, w, q.say[j], q.sby[j]);
+    if (jp != j) line[jp] = cosine_bwd(w, v, q.say[jp], q.sby[jp]);
+  }
+  __syncthreads();
+  smem_fft<1, double>(buf, ls, n, nl, q.twy_i);
+  for (int e = threadIdx.x; e < lanes * n; e += FFT_THREADS) {
+    const int r = e / lanes, l = e - r * lanes;
+    const int dst = (r < nh) ? 2 * r : 2 * n - 2 * r - 1;
+    if (l < nl) base[dst * rs + l] = buf[l * ls + r];
+  }
+}
+
+}  // namespace
+
+// Device tables of poisson_010 (one block of doubles):
+//   yk2 | ty | yky | say | sby (nym each) | twy_f | twy_i (2*nym each);
+// the stretching constants xa0, xa1 stay on the host (kernel arguments).
+static int p010_setup(Ctx* c) {
+  if (c->d_p010) return X3D_OK;
+  const AxisCoef& ay = c->ax[1];
+  const int nym = ay.nm;
+  dvec yky, yk2, tr, sa, sb;
+  waves_y010(ay, c->st.istret, c->grid.yly, yky, yk2, tr, sa, sb);
+  dvec h;
+  h.insert(h.end(), yk2.begin(), yk2.begin() + nym);
+  h.insert(h.end(), tr.begin(), tr.end());
+  h.insert(h.end(), yky.begin(), yky.begin() + nym);
+  h.insert(h.end(), sa.begin(), sa.end());
+  h.insert(h.end(), sb.begin(), sb.end());
+  std::vector<double> tw;
+  twiddles(nym, -1, tw);
+  twiddles(nym, +1, tw);
+  h.insert(h.end(), tw.begin(), tw.end());
+  const double pi = std::acos(-1.0), alpha = c->st.alpha, beta = c->st.beta;
+  double xa0 = 0, xa1 = 0;
+  if (c->st.istret == 1 || c->st.istret == 2) {
+    xa0 = alpha / pi + 0.5 / beta / pi;
+    xa1 = (c->st.istret == 1) ? 1.0 / 4.0 / beta / pi : -(1.0 / 4.0 / beta / pi);
+  }
+  c->p010_xa[0] = xa0;
+  c->p010_xa[1] = xa1;
+  double* d = nullptr;
+  if (cudaMalloc(&d, h.size() * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
+  cudaError_t e = cudaMemcpy(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(d);
+    return cuda_status(e);
+  }
+  c->d_p010 = d;
+  return X3D_OK;
+}
+
+int poisson_010(Ctx* c, double* rhs, cudaStream_t st) {
+  const int nx = c->grid.nx, nz = c->grid.nz, nym = c->ax[1].nm;
+  if (!c->ax[0].periodic || c->ax[1].periodic || !c->ax[2].periodic) return X3D_ERR_BC;
+  if (c->st.istret == 3) return X3D_ERR_UNSUPPORTED;  // inversion5_v2 path
+  if (!pow2(nx) || !pow2(nz) || !pow2(nym) || nx < 16 || nz < 8 || nym < 8) return X3D_ERR_UNSUPPORTED;
+  if (nx / 2 > FFT_ELEMS || nz > FFT_ELEMS || nym > 1024 || nz > 65535) return X3D_ERR_UNSUPPORTED;
+  int rc = fft_setup(c);
+  if (rc == X3D_OK) rc = p010_setup(c);
+  if (rc != X3D_OK) return rc;
+  typedef double2 C;
+  const int M = nx / 2, nxh = M + 1, ny = c->grid.ny;
+  const size_t need = (size_t)nxh * nym * nz * sizeof(C);
+  if (c->fft_work_bytes < need) {
+    if (c->fft_work) cudaFree(c->fft_work);
+    c->fft_work = nullptr;
+    c->fft_work_bytes = 0;
+    if (cudaMalloc(&c->fft_work, need) != cudaSuccess) return X3D_ERR_NOMEM;
+    c->fft_work_bytes = need;
+  }
+  C* spec = reinterpret_cast<C*>(c->fft_work);
+  const C* tw = reinterpret_cast<const C*>(c->d_twid);
+  const C* twx_f = tw;
+  const C* twx_i = tw + M;
+  const C* twx_full = tw + 2 * M;
+  const C* twz_f = twx_full + nxh + 2 * ny;
+  const C* twz_i = twz_f + nz;
+  P010 q;
+  const double* t = c->d_p010;
+  q.kx2 = c->d_k2[0]; q.trx = c->d_tr[0]; q.kz2 = c->d_k2[2]; q.trz = c->d_tr[2];
+  q.yk2 = t; q.ty = t + nym; q.yky = t + 2 * nym; q.say = t + 3 * nym; q.sby = t + 4 * nym;
+  q.twy_f = reinterpret_cast<const double2*>(t + 5 * nym);
+  q.twy_i = q.twy_f + nym;
+  q.istret = c->st.istret;
+  q.nx = nx; q.nz = nz; q.nym = nym;
+  q.scale = 1.0 / ((double)nx * (double)nym * (double)nz);
+  q.xa0 = c->p010_xa[0];
+  q.xa1 = c->p010_xa[1];
+  Spec sp{};
+  // A: x r2c
+  const long long nlines = (long long)nym * nz;
+  const int lpb = std::max(1, FFT_ELEMS / std::max(M, 1));
+  const size_t smem_x = (size_t)lpb * M * sizeof(C);
+  const unsigned nbx = (unsigned)((nlines + lpb - 1) / lpb);
+  {
+    auto k = fft_x_r2c<double>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x);
+    k<<<nbx, FFT_THREADS, smem_x, st>>>(rhs, spec, nx, nlines, lpb, twx_f, twx_full);
+  }
+  // B: z forward; lines over kx, outer over y
+  const int lanes_z = std::max(1, std::min(32, FFT_ELEMS / nz));
+  const size_t smem_z = (size_t)lanes_z * (nz + 1) * sizeof(C);
+  const dim3 gz((nxh + lanes_z - 1) / lanes_z, nym);
+  {
+    auto k = fft_strided<double, false, -1>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_z);
+    k<<<gz, FFT_THREADS, smem_z, st>>>(spec, nz, (long long)nxh * nym, nxh, lanes_z, nxh, twz_f, twz_i, sp);
+  }
+  // C: y reorder + cosine transform + solve
+  {
+    const int nh = nym / 2;
+    int lanes = std::max(1, std::min(16, FFT_ELEMS / nym));
+    auto smem_of = [&](int ln) { return (size_t)ln * (nym + 1) * sizeof(C) + (size_t)(2 * ln) * 5 * nh * sizeof(double); };
+    while (lanes > 1 && smem_of(lanes) > 200 * 1024) lanes /= 2;
+    const size_t smem = smem_of(lanes);
+    q.nsolve = 2 * lanes;
+    cudaFuncSetAttribute(k_p010_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const dim3 g((nxh + lanes - 1) / lanes, nz);
+    k_p010_y<<<g, FFT_THREADS, smem, st>>>(spec, nxh, nxh, lanes, (long long)nxh * nym, q);
+  }
+  // D: z inverse
+  {
+    auto k = fft_strided<double, false, 1>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_z);
+    k<<<gz, FFT_THREADS, smem_z, st>>>(spec, nz, (long long)nxh * nym, nxh, lanes_z, nxh, twz_f, twz_i, sp);
+  }
+  // E: x c2r
+  {
+    auto k = fft_x_c2r<double>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x);
+    k<<<nbx, FFT_THREADS, smem_x, st>>>(spec, rhs, nx, nlines, lpb, twx_i, twx_full);
+  }
+  return cuda_status(cudaGetLastError());
+}
+
 }  // namespace x3d

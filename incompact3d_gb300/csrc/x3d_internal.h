@@ -85,6 +85,19 @@ void coef_indices(const AxisCoef& a, int kind, int coefset, int* fi, int* si, in
 // Poisson tables (periodic): modified wavenumber^2 and interpolation transfer.
 void waves_tables(const AxisCoef& a, dvec& k2, dvec& tr);
 
+// Mesh stretching in y and its device copies.
+struct Stretch {
+  int istret = 0;
+  double beta = 0, alpha = 0;
+  dvec yp, ypi, ppy, pp2y, pp4y, ppyi, pp2yi, pp4yi;
+  double* d_ppy = nullptr;  // device: ppy | pp2y | pp4y | ppyi (ny each)
+};
+// Stretching metrics (src/stretching.f90) or the uniform defaults.
+int build_stretch(const x3d_grid& g, const AxisCoef& ay, Stretch& st);
+// poisson_010 tables of a non-periodic y axis: yky, yk2 (ny entries), the
+// transfer function (nym) and the shift factors sin/cos((j-1) pi/(2 nym)).
+void waves_y010(const AxisCoef& a, int istret, double yly, dvec& yky, dvec& yk2, dvec& tr, dvec& sa, dvec& sb);
+
 // Device scratch owned by a context, grown on demand (used by the stand-alone
 // projection entry points, which have no solver to borrow work fields from).
 struct Workspace {
@@ -114,9 +127,17 @@ struct Ctx {
   int twid_n = 0;
   void* fft_work = nullptr;  // complex spectrum buffer
   size_t fft_work_bytes = 0;
+  Stretch st;
+  double* d_p010 = nullptr;  // poisson_010 tables (see x3d_fft.cu)
+  double p010_xa[2] = {0, 0};  // stretching constants xa0, xa1 of matrice_refinement
   std::unique_ptr<Workspace> ws;
   ~Ctx();
 };
+
+// Device copies of ppy | pp2y | pp4y | ppyi (uploaded on first use).
+int stretch_device(Ctx* c, const double** out);
+// poisson_010 (x, z periodic; y non-periodic, stretched or not), FP64.
+int poisson_010(Ctx* c, double* rhs, cudaStream_t st);
 
 // Device scratch of at least `bytes` bytes (contents undefined).
 int ctx_workspace(Ctx* c, size_t bytes, void** out);

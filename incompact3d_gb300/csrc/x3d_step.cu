@@ -194,6 +194,100 @@ __global__ void k_absmax(const double* a, long long n, double* part) {
 
 }  // namespace
 
+// ---- channel case (walls at y = 0 and y = Ly, x and z periodic) -------------
+// channel_cfr (src/Case-Channel.f90:221-264): block partial sums of u/ppy(j).
+__global__ void k_cfr_partial(const double* ux, const double* ppy, int nx, int ny, long long n, double* part) {
+  __shared__ double sh[256];
+  double acc = 0.0;
+  GRID_STRIDE(m, n) {
+    const int j = (int)((m / nx) % ny);
+    acc += ux[m] / ppy[j];
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+// ub = sum * coeff; can = -(target - ub); ub and can go to out[0], out[1].
+__global__ void k_cfr_finish(const double* part, int nparts, double coeff, double target, double* out) {
+  __shared__ double sh[256];
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < nparts; b += 256) acc += part[b];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double ub = sh[0] * coeff;
+    out[0] = ub;
+    out[1] = -(target - ub);
+  }
+}
+__global__ void k_sub_dev(double* u, const double* c, long long n) {
+  const double v = *c;
+  GRID_STRIDE(i, n) u[i] = u[i] - v;
+}
+// momentum_forcing_channel rotation (src/Case-Channel.f90:413-418)
+__global__ void k_rotation(double* hx, double* hy, const double* ux, const double* uy, double w, long long n) {
+  GRID_STRIDE(i, n) {
+    const double a = hx[i] - w * uy[i];
+    const double b = hy[i] + w * ux[i];
+    hx[i] = a;
+    hy[i] = b;
+  }
+}
+// Stretched-mesh y-viscous term folded into the running sum
+// (src/transeq.f90:335-370 and 426-430):
+//   tz = xnu * (dyy * pp2y(j) - pp4y(j) * dy) + (tz - th/2)
+__global__ void k_visc_y_stretch(double* tz, const double* dyy, const double* dy, const double* th,
+                                 const double* pp2y, const double* pp4y, double xnu, int nx, int ny, long long n) {
+  GRID_STRIDE(m, n) {
+    const int j = (int)((m / nx) % ny);
+    const double td = dyy[m] * pp2y[j] - pp4y[j] * dy[m];
+    tz[m] = xnu * td + (tz[m] - 0.5 * th[m]);
+  }
+}
+// pre_correc no-slip walls (src/navier.f90:614-700): the stored tangential
+// pressure gradients are rescaled by gdt and imposed as the wall velocity.
+__global__ void k_walls(double* ux, double* uy, double* uz, double* dp, double g, int nx, int ny, int nz) {
+  const long long nw = (long long)nx * nz;
+  double* dpdx1 = dp;
+  double* dpdz1 = dp + nw;
+  double* dpdxn = dp + 2 * nw;
+  double* dpdzn = dp + 3 * nw;
+  GRID_STRIDE(w, nw) {
+    const long long i = w % nx, k = w / nx;
+    dpdx1[w] = dpdx1[w] * g;
+    dpdz1[w] = dpdz1[w] * g;
+    dpdxn[w] = dpdxn[w] * g;
+    dpdzn[w] = dpdzn[w] * g;
+    const long long b = i + (long long)nx * ny * k, t = b + (long long)nx * (ny - 1);
+    ux[b] = 0.0 + dpdx1[w];
+    uy[b] = 0.0;
+    uz[b] = 0.0 + dpdz1[w];
+    ux[t] = 0.0 + dpdxn[w];
+    uy[t] = 0.0;
+    uz[t] = 0.0 + dpdzn[w];
+  }
+}
+// gradp's wall-gradient storage (src/navier.f90:456-477)
+__global__ void k_wallgrad(double* dp, const double* px, const double* pz, double g, int nx, int ny, int nz) {
+  const long long nw = (long long)nx * nz;
+  GRID_STRIDE(w, nw) {
+    const long long i = w % nx, k = w / nx;
+    const long long b = i + (long long)nx * ny * k, t = b + (long long)nx * (ny - 1);
+    dp[w] = px[b] / g;
+    dp[nw + w] = pz[b] / g;
+    dp[2 * nw + w] = px[t] / g;
+    dp[3 * nw + w] = pz[t] / g;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Solver
 // ---------------------------------------------------------------------------
@@ -218,6 +312,13 @@ struct SolverImpl {
   double* part = nullptr;  // reduction partials
   double* hpart = nullptr;
   int launches = 0;
+  // channel case: walls in y (x, z periodic)
+  bool walls = false;       // geometry: y non-periodic with ncl 2/2
+  bool cfr = false;         // constant flow rate control (channel_cfr)
+  double cfr_target = 2.0 / 3.0, wrotation = 0.0;
+  int spinup_time = 0;
+  double* wall_dp = nullptr;  // dpdxy1 | dpdzy1 | dpdxyn | dpdzyn (nx*nz each)
+  double* ub_dev = nullptr;   // per sub-step: ub, can (2 x nsub)
   std::vector<void*> allocs;
   ~SolverImpl() {
     for (void* p : allocs) cudaFree(p);
@@ -243,12 +344,22 @@ namespace x3d {
 
 template <typename T>
 static int op(SolverImpl* s, int axis, int kind, int npaire, T* out, const T* in, const int* dims, cudaStream_t st,
-              const Fuse<T>* fz = nullptr) {
+              const Fuse<T>* fz = nullptr, const T* pp = nullptr) {
   OpPlan* p = nullptr;
   int rc = get_plan(s->c, axis, kind, npaire, default_coefset(kind, npaire), &p);
   if (rc != X3D_OK) return rc;
   s->launches++;
-  return launch_line_op<T>(s->c, p, out, in, dims, nullptr, st, fz);
+  return launch_line_op<T>(s->c, p, out, in, dims, pp, st, fz);
+}
+
+// y metric of a stretched mesh for operators in precision T (FP64 only):
+// which 0 = ppy, 1 = pp2y, 2 = pp4y, 3 = ppyi; null on a uniform mesh.
+template <typename T>
+static const T* ymetric(SolverImpl* s, int which) {
+  if (s->c->st.istret == 0 || !std::is_same<T, double>::value) return nullptr;
+  const double* d = nullptr;
+  if (stretch_device(s->c, &d) != X3D_OK) return nullptr;
+  return reinterpret_cast<const T*>(d + (size_t)which * s->c->grid.ny);
 }
 
 template <typename T>
@@ -292,6 +403,8 @@ static int momentum_rhs(SolverImpl* s, const T* const* u, T* const* H, cudaStrea
   T *t1 = w[0], *tg = w[1], *th = w[2], *tz = w[3];
   const T xnu = (T)s->o.xnu;
   const T one = T(1), mhalf = T(-0.5), zero = T(0);
+  // stretched mesh: dery multiplies by ppy; d2/dy2 gets the pp2y / pp4y terms
+  const T* ppy = ymetric<T>(s, 0);
   for (int q = 0; q < 3; ++q) {
     const T* uq = u[q];
     const int pu[3] = {q == 0 ? 0 : 1, q == 1 ? 0 : 1, q == 2 ? 0 : 1};  // parity of d_j u_q
@@ -303,9 +416,9 @@ static int momentum_rhs(SolverImpl* s, const T* const* u, T* const* H, cudaStrea
     RC(op<T>(s, 0, K_DER1, pu[0], tg, uq, dims, st, &f));
     // Y
     f = fz_prod<T>(uq);
-    RC(op<T>(s, 1, K_DER1, 1 - pu[1], t1, u[1], dims, st, &f));
+    RC(op<T>(s, 1, K_DER1, 1 - pu[1], t1, u[1], dims, st, &f, ppy));
     f = fz_comb<T>(zero, t1, one, nullptr, zero, u[1]);
-    RC(op<T>(s, 1, K_DER1, pu[1], th, uq, dims, st, &f));
+    RC(op<T>(s, 1, K_DER1, pu[1], th, uq, dims, st, &f, ppy));
     // Z
     f = fz_prod<T>(uq);
     RC(op<T>(s, 2, K_DER1, 1 - pu[2], t1, u[2], dims, st, &f));
@@ -314,8 +427,20 @@ static int momentum_rhs(SolverImpl* s, const T* const* u, T* const* H, cudaStrea
     f = fz_comb<T>(xnu, tz, mhalf, nullptr, zero, nullptr);
     RC(op<T>(s, 2, K_DER2, pu[2], tz, uq, dims, st, &f));
     // back to Y
-    f = fz_comb<T>(xnu, tz, one, th, mhalf, nullptr);
-    RC(op<T>(s, 1, K_DER2, pu[1], tz, uq, dims, st, &f));
+    if (ppy) {
+      T *tdy = w[5], *tdd = w[6];
+      RC(op<T>(s, 1, K_DER1, pu[1], tdy, uq, dims, st, nullptr, ppy));
+      RC(op<T>(s, 1, K_DER2, pu[1], tdd, uq, dims, st));
+      const long long N = s->N;
+      k_visc_y_stretch<<<pw_blocks(c, N), 256, 0, st>>>((double*)tz, (const double*)tdd, (const double*)tdy,
+                                                        (const double*)th, (const double*)ymetric<T>(s, 1),
+                                                        (const double*)ymetric<T>(s, 2), s->o.xnu, c->grid.nx,
+                                                        c->grid.ny, N);
+      s->launches++;
+    } else {
+      f = fz_comb<T>(xnu, tz, one, th, mhalf, nullptr);
+      RC(op<T>(s, 1, K_DER2, pu[1], tz, uq, dims, st, &f));
+    }
     // back to X: final sum into the history slot
     f = fz_comb<T>(xnu, tz, one, tg, mhalf, nullptr);
     RC(op<T>(s, 0, K_DER2, pu[0], H[q], uq, dims, st, &f));
@@ -338,7 +463,7 @@ static int divergence(SolverImpl* s, const T* ux, const T* uy, const T* uz, doub
   RC(op<T>(s, 0, K_IVP, 1, pgz1, uz, d1, st));
   const int d2[3] = {nxm, ny, nz};
   RC(op<T>(s, 1, K_IVP, 1, upi2, pp1, d2, st));
-  RC(op<T>(s, 1, K_DVP, 0, duy, pgy1, d2, st));
+  RC(op<T>(s, 1, K_DVP, 0, duy, pgy1, d2, st, nullptr, ymetric<T>(s, 3)));
   const long long n2 = (long long)nxm * c->ax[1].nm * nz;
   k_add<T><<<pw_blocks(c, n2), 256, 0, st>>>(duy, duy, upi2, n2);
   s->launches++;
@@ -351,7 +476,8 @@ static int divergence(SolverImpl* s, const T* ux, const T* uy, const T* uz, doub
   return cuda_status(cudaGetLastError());
 }
 
-// gradp of src/navier.f90:386-499 (periodic: no wall-gradient storage).
+// gradp of src/navier.f90:386-432 (the wall-gradient storage of the channel
+// case is done by the caller).
 template <typename T>
 static int gradp(SolverImpl* s, const T* pp3, T* px, T* py, T* pz, cudaStream_t st) {
   Ctx* c = s->c;
@@ -364,13 +490,21 @@ static int gradp(SolverImpl* s, const T* pp3, T* px, T* py, T* pz, cudaStream_t 
   RC(op<T>(s, 2, K_DPV, 1, pgz3, pp3, d3, st));
   const int d2[3] = {nxm, nym, nz};
   RC(op<T>(s, 1, K_IPV, 1, ppi2, ppi3, d2, st));
-  RC(op<T>(s, 1, K_DPV, 1, pgy2, ppi3, d2, st));
+  RC(op<T>(s, 1, K_DPV, 1, pgy2, ppi3, d2, st, nullptr, ymetric<T>(s, 0)));
   RC(op<T>(s, 1, K_IPV, 1, pgzi2, pgz3, d2, st));
   const int d1[3] = {nxm, ny, nz};
   RC(op<T>(s, 0, K_DPV, 1, px, ppi2, d1, st));
   RC(op<T>(s, 0, K_IPV, 1, py, pgy2, d1, st));
   RC(op<T>(s, 0, K_IPV, 1, pz, pgzi2, d1, st));
   return X3D_OK;
+}
+
+// ppy as channel_cfr divides by it: the stretching metric, or on a uniform
+// mesh the default 1 with 2 at the walls (src/variables.f90:1294-1305).
+static const double* ymetric_cfr(SolverImpl* s) {
+  const double* d = nullptr;
+  if (stretch_device(s->c, &d) != X3D_OK) return nullptr;
+  return d;
 }
 
 template <typename T>
@@ -383,9 +517,22 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
   const T* u[3];
   for (int q = 0; q < 3; ++q) u[q] = mixed ? (const T*)s->uh[q] : (const T*)(q == 0 ? s->ux : q == 1 ? s->uy : s->uz);
   T* H[3] = {(T*)s->H[0][0], (T*)s->H[1][0], (T*)s->H[2][0]};
+  const int it = s->itime + 1;  // 1-based step index
+  if (s->cfr) {
+    // boundary_conditions -> channel_cfr on ux, before the right-hand side
+    const int np = 2 * c->num_sms;
+    k_cfr_partial<<<np, 256, 0, st>>>(s->ux, ymetric_cfr(s), c->grid.nx, c->grid.ny, N, s->part);
+    const double coeff = c->ax[1].d / (c->grid.yly * (double)(c->grid.nx * c->grid.nz));
+    k_cfr_finish<<<1, 256, 0, st>>>(s->part, np, coeff, s->cfr_target, s->ub_dev + 2 * (itr - 1));
+    k_sub_dev<<<nb, 256, 0, st>>>(s->ux, s->ub_dev + 2 * (itr - 1) + 1, N);
+    s->launches += 3;
+  }
   RC(momentum_rhs<T>(s, u, H, st));
-  // intt (src/time_integrators.f90:18-187); itime is the 1-based step index
-  const int it = s->itime + 1;
+  if (s->walls && s->wrotation != 0.0 && it < s->spinup_time) {
+    k_rotation<<<nb, 256, 0, st>>>((double*)H[0], (double*)H[1], s->ux, s->uy, s->wrotation, N);
+    s->launches++;
+  }
+  // intt (src/time_integrators.f90:18-187)
   const double dt = s->o.dt;
   double c1 = 0, c2 = 0, c3 = 0;
   int nh = 1;
@@ -428,10 +575,20 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
     }
   }
   RC(cuda_status(cudaGetLastError()));
+  const double g = s->gdt[s->o.itimescheme == 3 ? 0 : itr - 1];
+  if (s->walls) {
+    k_walls<<<pw_blocks(c, (long long)c->grid.nx * c->grid.nz), 256, 0, st>>>(
+        s->ux, s->uy, s->uz, s->wall_dp, g, c->grid.nx, c->grid.ny, c->grid.nz);
+    s->launches++;
+  }
   // projection: divergence, Poisson, gradient, correction
   RC(divergence<T>(s, u[0], u[1], u[2], s->pp64, st));
-  // mixed: FP64-class Poisson solve in double-float arithmetic on the FP32 pipes
-  RC(poisson_periodic(c, s->pp64, mixed ? 2 : 0, st));
+  if (s->walls) {
+    RC(poisson_010(c, s->pp64, st));
+  } else {
+    // mixed: FP64-class Poisson solve in double-float arithmetic on the FP32 pipes
+    RC(poisson_periodic(c, s->pp64, mixed ? 2 : 0, st));
+  }
   s->launches += 5;
   const T* pin = (const T*)s->pp64;
   T** w = reinterpret_cast<T**>(s->W);
@@ -441,6 +598,11 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
     pin = (const T*)w[4];
   }
   RC(gradp<T>(s, pin, w[0], w[1], w[2], st));
+  if (s->walls) {
+    k_wallgrad<<<pw_blocks(c, (long long)c->grid.nx * c->grid.nz), 256, 0, st>>>(
+        s->wall_dp, (const double*)w[0], (const double*)w[2], g, c->grid.nx, c->grid.ny, c->grid.nz);
+    s->launches++;
+  }
   if (mixed) {
     Cor3 a;
     for (int q = 0; q < 3; ++q) {
@@ -478,9 +640,18 @@ static int solver_alloc(SolverImpl* s) {
       if (!s->H[q][k]) return X3D_ERR_NOMEM;
       cudaMemset(s->H[q][k], 0, (size_t)N * es);
     }
-  for (int k = 0; k < 5; ++k) {
+  const int nw = (c->st.istret != 0) ? 7 : 5;
+  for (int k = 0; k < nw; ++k) {
     s->W[k] = s->alloc<unsigned char>(N * (long long)es);
     if (!s->W[k]) return X3D_ERR_NOMEM;
+  }
+  if (s->walls) {
+    const long long nwall = 4LL * c->grid.nx * c->grid.nz;
+    s->wall_dp = s->alloc<double>(nwall);
+    s->ub_dev = s->alloc<double>(6);
+    if (!s->wall_dp || !s->ub_dev) return X3D_ERR_NOMEM;
+    cudaMemset(s->wall_dp, 0, (size_t)nwall * sizeof(double));
+    cudaMemset(s->ub_dev, 0, 6 * sizeof(double));
   }
   for (int k = 0; k < 7; ++k) {
     s->P[k] = s->alloc<unsigned char>(N * (long long)es);
@@ -490,7 +661,6 @@ static int solver_alloc(SolverImpl* s) {
   s->part = s->alloc<double>(4LL * 4096);
   if (!s->pp64 || !s->part) return X3D_ERR_NOMEM;
   if (cudaMallocHost(&s->hpart, 4 * 4096 * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
-  (void)c;
   return cuda_status(cudaGetLastError());
 }
 
@@ -503,13 +673,20 @@ extern "C" {
 int x3d_solver_create(x3d_ctx* ctx_, const x3d_solver_opts* o, x3d_solver** out) {
   if (!ctx_ || !o || !out) return X3D_ERR_ARG;
   Ctx* c = reinterpret_cast<Ctx*>(ctx_);
-  if (!c->ax[0].periodic || !c->ax[1].periodic || !c->ax[2].periodic) return X3D_ERR_BC;
+  const bool periodic = c->ax[0].periodic && c->ax[1].periodic && c->ax[2].periodic;
+  // channel geometry: x, z periodic, no-slip walls at both y ends
+  const bool walls = c->ax[0].periodic && c->ax[2].periodic && !c->ax[1].periodic && c->ax[1].ncl1 == 2 &&
+                     c->ax[1].ncln == 2;
+  if (!periodic && !walls) return X3D_ERR_BC;
   if (o->itimescheme != 3 && o->itimescheme != 5) return X3D_ERR_UNSUPPORTED;
   if (o->precision != X3D_PREC_FP64 && o->precision != X3D_PREC_MIXED) return X3D_ERR_DTYPE;
+  if (walls && o->precision != X3D_PREC_FP64) return X3D_ERR_DTYPE;
+  if (walls && c->st.istret == 3) return X3D_ERR_UNSUPPORTED;
   x3d_solver* s = new x3d_solver();
   SolverImpl* si = &s->impl;
   si->c = c;
   si->o = *o;
+  si->walls = walls;
   si->N = (long long)c->grid.nx * c->grid.ny * c->grid.nz;
   si->Np = (long long)c->ax[0].nm * c->ax[1].nm * c->ax[2].nm;
   const double dt = o->dt;
@@ -535,6 +712,29 @@ int x3d_solver_create(x3d_ctx* ctx_, const x3d_solver_opts* o, x3d_solver** out)
 int x3d_solver_destroy(x3d_solver* s) {
   delete s;
   return X3D_OK;
+}
+
+int x3d_solver_set_channel(x3d_solver* s, double target_ub, double wrotation, int spinup_time) {
+  if (!s) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  if (!si->walls) return X3D_ERR_BC;
+  si->cfr = true;
+  si->cfr_target = target_ub;
+  si->wrotation = wrotation;
+  si->spinup_time = spinup_time;
+  return X3D_OK;
+}
+
+int x3d_solver_bulk_velocity(x3d_solver* s, double* out, int capacity) {
+  if (!s || !out) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  if (!si->cfr) return X3D_ERR_STATE;
+  if (capacity < si->nsub) return X3D_ERR_ARG;
+  double h[6];
+  int rc = cuda_status(cudaMemcpy(h, si->ub_dev, sizeof(h), cudaMemcpyDeviceToHost));
+  if (rc != X3D_OK) return rc;
+  for (int k = 0; k < si->nsub; ++k) out[k] = h[2 * k];
+  return si->nsub;
 }
 
 // After the FP64 staging arrays change: derive the double-float state.

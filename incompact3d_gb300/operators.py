@@ -55,10 +55,10 @@ class Context:
     """Grid + numerical options; owns the coefficient tables in HBM."""
 
     def __init__(self, nx, ny, nz, xlx, yly, zlz, bc=((0, 0), (0, 0), (0, 0)), ifirstder=4,
-                 isecondder=4, ipinter=3, filter_alpha=0.49, nu0nu=4.0, cnu=0.44, istret=0):
+                 isecondder=4, ipinter=3, filter_alpha=0.49, nu0nu=4.0, cnu=0.44, istret=0, beta=0.0):
         self.lib = _lib.load()
         g = _lib.Grid(nx, ny, nz, xlx, yly, zlz, bc[0][0], bc[0][1], bc[1][0], bc[1][1],
-                      bc[2][0], bc[2][1], istret, 0.0)
+                      bc[2][0], bc[2][1], istret, beta)
         o = _lib.NumOpts(ifirstder, isecondder, ipinter, filter_alpha, nu0nu, cnu)
         h = ctypes.c_void_p()
         check(self.lib.x3d_ctx_create(ctypes.byref(g), ctypes.byref(o), ctypes.byref(h)), "x3d_ctx_create")
@@ -77,6 +77,21 @@ class Context:
             self.close()
         except Exception:
             pass
+
+    STRETCH_NAMES = ("yp", "ypi", "ppy", "pp2y", "pp4y", "ppyi", "pp2yi", "pp4yi")
+
+    def stretching(self):
+        """y-mesh metrics (dict of host arrays) and the mapping constant alpha."""
+        out = {}
+        buf = np.zeros(self.n[1] + 8)
+        for w, nm in enumerate(self.STRETCH_NAMES):
+            k = check(self.lib.x3d_get_stretching(self.h, w, buf.ctypes.data_as(ctypes.c_void_p), buf.size),
+                      "x3d_get_stretching")
+            out[nm] = buf[:k].copy()
+        check(self.lib.x3d_get_stretching(self.h, 8, buf.ctypes.data_as(ctypes.c_void_p), buf.size),
+              "x3d_get_stretching")
+        out["alpha"] = float(buf[0])
+        return out
 
     # ---- coefficient vectors (host copies, as the reference passes them) ----
     def coeffs(self, axis, name):
@@ -127,7 +142,8 @@ class Context:
     def dery(self, ty, uy, ry=None, sy=None, ffy=None, fsy=None, fwy=None, ppy=None, nx=None, ny=None,
              nz=None, npaire=0, lind=0.0):
         nx, ny, nz = self._dims(nx, ny, nz)
-        return self._colloc(self.lib.x3d_dery, ty, uy, ffy, fsy, fwy, nx, ny, nz, npaire, None)
+        hp = _hptr(ppy)  # NULL: the context's ppy (applied only on a stretched mesh)
+        return self._colloc(self.lib.x3d_dery, ty, uy, ffy, fsy, fwy, nx, ny, nz, npaire, hp[0] if hp else None)
 
     def derz(self, tz, uz, rz=None, sz=None, ffz=None, fsz=None, fwz=None, nx=None, ny=None, nz=None,
              npaire=0, lind=0.0):
@@ -255,6 +271,18 @@ class Solver:
         on_dev = 0 if isinstance(ux, np.ndarray) or not getattr(ux, "is_cuda", False) else 1
         check(self.lib.x3d_solver_get_velocity(self.h, addr(ux), addr(uy), addr(uz), on_dev),
               "x3d_solver_get_velocity")
+
+    def set_channel(self, target_ub=2.0 / 3.0, wrotation=0.0, spinup_time=0):
+        """Channel case: constant flow rate control and the spin-up rotation."""
+        check(self.lib.x3d_solver_set_channel(self.h, target_ub, wrotation, spinup_time),
+              "x3d_solver_set_channel")
+
+    def bulk_velocity(self):
+        """Bulk velocity seen by the flow-rate control at each sub-step of the last step."""
+        out = np.zeros(8)
+        n = check(self.lib.x3d_solver_bulk_velocity(self.h, out.ctypes.data_as(ctypes.c_void_p), out.size),
+                  "x3d_solver_bulk_velocity")
+        return out[:n].copy()
 
     def init_tgv(self):
         check(self.lib.x3d_solver_init_tgv(self.h), "x3d_solver_init_tgv")

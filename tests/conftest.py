@@ -22,6 +22,15 @@ def oracle_mod():
 
 
 @pytest.fixture(scope="session")
+def gpu_lib_host():
+    """Built library for host-side calls (context tables); no device needed."""
+    import incompact3d_gb300 as x3d
+    x3d.build()
+    x3d.load()
+    return x3d
+
+
+@pytest.fixture(scope="session")
 def gpu_lib():
     """Built library + a CUDA device; the library is the only compute path."""
     torch = pytest.importorskip("torch")

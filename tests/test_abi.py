@@ -53,9 +53,14 @@ def test_host_side_argument_checks(lib):
     # mixed periodic / non-periodic ends on one axis
     g = _lib.Grid(16, 16, 16, L, L, L, 0, 2, 0, 0, 0, 0, 0, 0.0)
     assert so.x3d_ctx_create(ctypes.byref(g), ctypes.byref(o), ctypes.byref(h)) == -3
-    # stretching is outside the implemented scope
-    g = _lib.Grid(16, 16, 16, L, L, L, 0, 0, 2, 2, 0, 0, 2, 0.259)
+    # stretching needs a non-periodic y (src/parameters.f90:283); istret is 0..3
+    g = _lib.Grid(16, 16, 16, L, L, L, 0, 0, 0, 0, 0, 0, 2, 0.259)
+    assert so.x3d_ctx_create(ctypes.byref(g), ctypes.byref(o), ctypes.byref(h)) == -3
+    g = _lib.Grid(16, 17, 16, L, L, L, 0, 0, 2, 2, 0, 0, 4, 0.259)
     assert so.x3d_ctx_create(ctypes.byref(g), ctypes.byref(o), ctypes.byref(h)) == -7
+    g = _lib.Grid(16, 17, 16, L, L, L, 0, 0, 2, 2, 0, 0, 2, 0.259)
+    assert so.x3d_ctx_create(ctypes.byref(g), ctypes.byref(o), ctypes.byref(h)) == 0
+    so.x3d_ctx_destroy(h)
     # too small
     g = _lib.Grid(4, 16, 16, L, L, L, 0, 0, 0, 0, 0, 0, 0, 0.0)
     assert so.x3d_ctx_create(ctypes.byref(g), ctypes.byref(o), ctypes.byref(h)) == -2

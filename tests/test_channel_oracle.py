@@ -90,3 +90,17 @@ def test_channel_projection_and_flow_rate(oracle_mod, istret):
     assert abs(ub[-1] - 2.0 / 3.0) < 1e-5
     assert dmax < 1e-12
     assert np.all(b[:, 0, :] == 0) and np.all(b[:, -1, :] == 0)
+
+
+@pytest.mark.parametrize("istret", [0, 1, 2, 3])
+def test_library_stretching_tables_match_oracle(oracle_mod, gpu_lib_host, istret):
+    """The library's host-side stretching metrics equal the oracle's bit for bit
+    (no device needed: the context builds its tables on the host)."""
+    ny = 65
+    L = (8 * np.pi, 2.0, 3 * np.pi)
+    o = oracle_mod.Oracle(32, ny, 16, *L, bc=((0, 0), (2, 2), (0, 0)), istret=istret, beta=BETA)
+    ctx = gpu_lib_host.Context(32, ny, 16, *L, bc=((0, 0), (2, 2), (0, 0)), istret=istret, beta=BETA)
+    a, b = o.stretching(), ctx.stretching()
+    for k in ("yp", "ypi", "ppy", "pp2y", "pp4y", "ppyi", "pp2yi", "pp4yi"):
+        assert np.array_equal(a[k], b[k]), k
+    assert a["alpha"] == b["alpha"]
