@@ -9,6 +9,7 @@ with the kinetic-energy difference between the two after the same steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--n 512] [--impl ours|reference]
   python bench.py --workload ops [--n 512] [--ops dery,...] [--dtypes f64,f32] [--bcs 0,2]
+  python bench.py --workload channel [--steps K] [--warmup W]
 
 --impl reference times the CPU restatement of the reference's path (the
 parity oracle, C++/OpenMP on all host cores) on a bounded sample grid of the
@@ -369,10 +370,71 @@ def run_ops(args):
                   flush=True)
 
 
+CHANNEL_L = (8 * 3.141592653589793, 2.0, 3 * 3.141592653589793)
+CHANNEL_BETA = 0.259065151
+
+
+def channel_ic(np, nx, ny, nz, yp, Ly=2.0, noise=0.125, seed=20261204):
+    """Laminar Poiseuille profile plus modulated uniform noise (seeded PCG64)."""
+    rng = np.random.default_rng(seed)
+    y = yp - Ly / 2
+    um = np.exp(-0.2 * y * y)
+    r = [rng.uniform(size=(nz, ny, nx)) for _ in range(3)]
+    ux = noise * um[None, :, None] * (2 * r[0] - 1) + (1 - y * y)[None, :, None]
+    uy = noise * um[None, :, None] * (2 * r[1] - 1)
+    uz = noise * um[None, :, None] * (2 * r[2] - 1)
+    return ux, uy, uz
+
+
+def run_channel(args):
+    """Turbulent channel, FP64: 256x129x128 on 8pi x 2 x 3pi, y stretched at both
+    walls (istret=2, beta=0.259), constant flow rate, RK3, dt=0.002, Re=4200.
+    One JSON line: Mpts*steps/s of the GPU solver, with the CPU oracle timed
+    on a sample grid beside it."""
+    import numpy as np
+    import torch
+    import incompact3d_gb300 as x3d
+
+    x3d.build()
+    nx, ny, nz = 256, 129, 128
+    bc = ((0, 0), (2, 2), (0, 0))
+    ctx = x3d.Context(nx, ny, nz, *CHANNEL_L, bc=bc, istret=2, beta=CHANNEL_BETA)
+    s = x3d.Solver(ctx, 0.002, 1 / 4200.0, itimescheme=5, precision=x3d.PREC_FP64)
+    s.set_channel()
+    s.set_velocity(*channel_ic(np, nx, ny, nz, ctx.stretching()["yp"]))
+    s.step(args.warmup)
+    stream = torch.cuda.current_stream()
+    with Clocks(0) as clk:
+        secs = time_steps(torch, s, args.steps, stream)
+    N = nx * ny * nz
+    ub = s.bulk_velocity()
+    line = {"workload": "channel_256x129x128_rk3_fp64", "metric": "channel Mpts*steps/s", "unit": UNIT,
+            "value": round(N * args.steps / secs / 1e6, 3), "ms_per_step": round(1e3 * secs / args.steps, 3),
+            "steps": args.steps, "warmup": args.warmup, "dtype": "f64", "clocks": clk.summary(),
+            "launches_per_step": s.lib.x3d_solver_launches_per_step(s.h), "bulk_velocity": float(ub[-1]),
+            "divmax": s.divmax()}
+    if not args.no_cpu:
+        import oracle
+        oracle.build()
+        threads = oracle.Oracle.set_threads(os.cpu_count() or 1)
+        m = (64, 65, 32)
+        o = oracle.Oracle(*m, *CHANNEL_L, bc=bc, istret=2, beta=CHANNEL_BETA)
+        ic = channel_ic(np, *m, o.stretching()["yp"])
+        o.run_channel(*ic, 1, 0.002, 1 / 4200.0, itimescheme=5)
+        t0 = time.perf_counter()
+        o.run_channel(*ic, 2, 0.002, 1 / 4200.0, itimescheme=5)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": round(m[0] * m[1] * m[2] * 2 / dt / 1e6, 4), "unit": UNIT,
+                                "cores": threads, "kind": "port",
+                                "sample": "oracle channel 64x65x32, 2 RK3 steps, rate per grid point"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "ops"],
-                    help="tgv: the time-step benchmark (default); ops: operator microbench lines")
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "ops", "channel"],
+                    help="tgv: the time-step benchmark (default); ops: operator microbench lines; "
+                         "channel: the stretched turbulent channel (FP64)")
     ap.add_argument("--ops", default="", help="ops workload: comma list (derx,...,filz,poisson)")
     ap.add_argument("--dtypes", default="f64,f32")
     ap.add_argument("--bcs", default="0,2")
@@ -393,6 +455,8 @@ def main():
         args.warmup = 3
     if args.workload == "ops":
         run_ops(args)
+    elif args.workload == "channel":
+        run_channel(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

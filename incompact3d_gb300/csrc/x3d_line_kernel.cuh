@@ -316,9 +316,11 @@ template <typename T, int KIND>
 int dispatch_xl(const LineArgs<T>& a, bool xl, int lmax, dim3 grid, size_t smem, cudaStream_t st) {
   if (xl) {
     if (lmax == 8) return launch_k<T, KIND, true, 8>(a, grid, smem, st);
+    if (lmax == 16) return launch_k<T, KIND, true, 16>(a, grid, smem, st);
     return launch_k<T, KIND, true, 32>(a, grid, smem, st);
   }
   if (lmax == 8) return launch_k<T, KIND, false, 8>(a, grid, smem, st);
+  if (lmax == 16) return launch_k<T, KIND, false, 16>(a, grid, smem, st);
   return launch_k<T, KIND, false, 32>(a, grid, smem, st);
 }
 

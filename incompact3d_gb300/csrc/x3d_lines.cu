@@ -219,7 +219,7 @@ int launch_line_op(Ctx* c, OpPlan* p, T* out, const T* in, const int* dims_in, c
     }
   }
   if (fz) a.fz = *fz;
-  const int lmax = (p->L <= 8) ? 8 : 32;
+  const int lmax = (p->L <= 8) ? 8 : (p->L <= 16) ? 16 : 32;
   const size_t smem = line_smem<T>(p->nin, p->nout);
   if (smem > 227 * 1024) return X3D_ERR_UNSUPPORTED;
   return dispatch<T>(a, p->kind, xl, lmax, grid, smem, st);
