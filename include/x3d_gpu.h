@@ -311,6 +311,16 @@ int x3d_solver_launches_per_step(x3d_solver* s);
  * wall values of pre_correc and the wall pressure gradients of gradp are
  * always applied in the channel geometry.  X3D_ERR_BC on a periodic solver. */
 int x3d_solver_set_channel(x3d_solver* s, double target_ub, double wrotation, int spinup_time);
+/* Explicit LES in the right-hand side (compute_SGS, src/les_models.f90:96-165,
+ * iconserv = 0): jles = 1 Smagorinsky (smag, :168-331) with constant smagcst,
+ * jles = 3 dynamic Smagorinsky (dynsmag, :333-903; filters with alpha = 0 as
+ * its filter(zero) call sets, constant clipped to [0, maxdsmagcst]), 0 off.
+ * The force of sgs_mom_nonconservative (:1091-1250) is added to the momentum
+ * right-hand side.  FP64 solver only (X3D_ERR_DTYPE otherwise). */
+int x3d_solver_set_les(x3d_solver* s, int jles, double smagcst, double maxdsmagcst);
+/* Eddy viscosity and SGS force of the current velocity into device arrays of
+ * N = nx*ny*nz doubles (for checks and output), stream-ordered. */
+int x3d_solver_les_fields(x3d_solver* s, double* nut, double* sgsx, double* sgsy, double* sgsz, void* stream);
 /* Bulk velocity measured by channel_cfr (before its correction) at each
  * sub-step of the last step; returns the number of values.  Synchronises. */
 int x3d_solver_bulk_velocity(x3d_solver* s, double* out, int capacity);

@@ -288,6 +288,131 @@ __global__ void k_wallgrad(double* dp, const double* px, const double* pz, doubl
   }
 }
 
+// ---- explicit LES (src/les_models.f90) -----------------------------------
+__global__ void k_les_prod(double* p0, double* p1, double* p2, double* p3, double* p4, double* p5,
+                           const double* ux, const double* uy, const double* uz, long long n) {
+  GRID_STRIDE(m, n) {
+    const double a = ux[m], b = uy[m], c = uz[m];
+    p0[m] = a * a; p1[m] = b * b; p2[m] = c * c;
+    p3[m] = a * b; p4[m] = a * c; p5[m] = b * c;
+  }
+}
+struct Six {
+  double* v[6];
+};
+struct CSix {
+  const double* v[6];
+};
+// srt = S:S (smag, src/les_models.f90:265-267)
+__global__ void k_les_srt(double* srt, CSix S, long long n) {
+  GRID_STRIDE(m, n) {
+    const double xx = S.v[0][m], yy = S.v[1][m], zz = S.v[2][m], xy = S.v[3][m], xz = S.v[4][m], yz = S.v[5][m];
+    srt[m] = xx * xx + yy * yy + zz * zz + 2.0 * xy * xy + 2.0 * xz * xz + 2.0 * yz * yz;
+  }
+}
+// out_q = -2 sqrt(2 S:S) S_q * (f del(j))^2 (dynsmag's a_ij with f = 1 and
+// b_ij with f = 2, src/les_models.f90:609-676); out may alias S.
+__global__ void k_les_tensor(Six out, CSix S, const double* del, double f, int nx, int ny, long long n) {
+  GRID_STRIDE(m, n) {
+    const double xx = S.v[0][m], yy = S.v[1][m], zz = S.v[2][m], xy = S.v[3][m], xz = S.v[4][m], yz = S.v[5][m];
+    const double mag = sqrt(2.0 * (xx * xx + yy * yy + zz * zz + 2.0 * xy * xy + 2.0 * xz * xz + 2.0 * yz * yz));
+    const double dl = f * del[(m / nx) % ny];
+    const double d2 = dl * dl;
+    const double s6[6] = {xx, yy, zz, xy, xz, yz};
+#pragma unroll
+    for (int q = 0; q < 6; ++q) out.v[q][m] = (-2.0 * mag * s6[q]) * d2;
+  }
+}
+// L_ij = (u_i u_j)^f - u_i^f u_j^f, in place on the filtered products
+__global__ void k_les_leonard(Six P, const double* uf, const double* vf, const double* wf, long long n) {
+  GRID_STRIDE(m, n) {
+    const double a = uf[m], b = vf[m], c = wf[m];
+    P.v[0][m] = P.v[0][m] - a * a;
+    P.v[1][m] = P.v[1][m] - b * b;
+    P.v[2][m] = P.v[2][m] - c * c;
+    P.v[3][m] = P.v[3][m] - a * b;
+    P.v[4][m] = P.v[4][m] - a * c;
+    P.v[5][m] = P.v[5][m] - b * c;
+  }
+}
+// dynamic constant (src/les_models.f90:780-811): M = b - a^f, deviatoric L
+// (statement by statement as written), C = L:M / M:M clipped to [0, cmax]
+__global__ void k_les_smagc(double* C, CSix L, CSix B, CSix A, double cmax, long long n) {
+  GRID_STRIDE(m, n) {
+    const double mxx = B.v[0][m] - A.v[0][m], myy = B.v[1][m] - A.v[1][m], mzz = B.v[2][m] - A.v[2][m];
+    const double mxy = B.v[3][m] - A.v[3][m], mxz = B.v[4][m] - A.v[4][m], myz = B.v[5][m] - A.v[5][m];
+    double lxx = L.v[0][m], lyy = L.v[1][m], lzz = L.v[2][m];
+    const double lxy = L.v[3][m], lxz = L.v[4][m], lyz = L.v[5][m];
+    lxx = lxx - (lxx + lyy + lzz) / 3.0;
+    lyy = lyy - (lxx + lyy + lzz) / 3.0;
+    lzz = lzz - (lxx + lyy + lzz) / 3.0;
+    double v = (lxx * mxx + lyy * myy + lzz * mzz + 2.0 * (lxy * mxy + lxz * mxz + lyz * myz)) /
+               (mxx * mxx + myy * myy + mzz * mzz + 2.0 * (mxy * mxy + mxz * mxz + myz * myz));
+    if (v > cmax) v = cmax;
+    if (v < 0.0) v = 0.0;
+    C[m] = v;
+  }
+}
+// nut = <C>_z del(j)^2 sqrt(2 srt): mean over z per (x, y) column
+// (mean_plane_z, src/tools.f90:982-996), summed in k order
+__global__ void k_les_nut_dyn(double* nut, const double* cf, const double* srt, const double* del, int nx, int ny,
+                              int nz) {
+  const long long ncol = (long long)nx * ny;
+  GRID_STRIDE(col, ncol) {
+    const long long plane = ncol;
+    double sum = 0.0;
+    for (int k = 0; k < nz; ++k) sum = sum + cf[col + k * plane];
+    const double cm = sum / (double)nz;
+    const double dl = del[col / nx];
+    for (int k = 0; k < nz; ++k) {
+      const long long m = col + k * plane;
+      nut[m] = cm * (dl * dl) * sqrt(2.0 * srt[m]);
+    }
+  }
+}
+// smag: nut = (Cs del(j))^2 sqrt(2 srt)
+__global__ void k_les_nut_smag(double* nut, const double* srt, const double* del, double cs, int nx, int ny,
+                               long long n) {
+  GRID_STRIDE(m, n) {
+    const double length = cs * del[(m / nx) % ny];
+    nut[m] = (length * length) * sqrt(2.0 * srt[m]);
+  }
+}
+// sgs_mom_nonconservative terms of one direction (src/les_models.f90:1115-1232):
+//   g_q (+)= nut * d2_q + 2 S_q * dnut      (first = 1: assignment)
+__global__ void k_les_sgs(double* gx, double* gy, double* gz, const double* d2x, const double* d2y,
+                          const double* d2z, const double* nut, const double* dnut, const double* sa,
+                          const double* sb, const double* sc, int first, long long n) {
+  GRID_STRIDE(m, n) {
+    const double nu = nut[m], dn = dnut[m];
+    if (first) {
+      gx[m] = d2x[m] * nu + 2.0 * sa[m] * dn;
+      gy[m] = d2y[m] * nu + 2.0 * sb[m] * dn;
+      gz[m] = d2z[m] * nu + 2.0 * sc[m] * dn;
+    } else {
+      gx[m] = gx[m] + nu * d2x[m] + 2.0 * sa[m] * dn;
+      gy[m] = gy[m] + nu * d2y[m] + 2.0 * sb[m] * dn;
+      gz[m] = gz[m] + nu * d2z[m] + 2.0 * sc[m] * dn;
+    }
+  }
+}
+// stretched-mesh second derivative: t = t pp2y(j) - pp4y(j) dy
+__global__ void k_stretch_d2(double* t, const double* dy, const double* pp2y, const double* pp4y, int nx, int ny,
+                             long long n) {
+  GRID_STRIDE(m, n) {
+    const int j = (int)((m / nx) % ny);
+    t[m] = t[m] * pp2y[j] - pp4y[j] * dy[m];
+  }
+}
+__global__ void k_add3(double* hx, double* hy, double* hz, const double* gx, const double* gy, const double* gz,
+                       long long n) {
+  GRID_STRIDE(m, n) {
+    hx[m] = hx[m] + gx[m];
+    hy[m] = hy[m] + gy[m];
+    hz[m] = hz[m] + gz[m];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Solver
 // ---------------------------------------------------------------------------
@@ -319,10 +444,17 @@ struct SolverImpl {
   int spinup_time = 0;
   double* wall_dp = nullptr;  // dpdxy1 | dpdzy1 | dpdxyn | dpdzyn (nx*nz each)
   double* ub_dev = nullptr;   // per sub-step: ub, can (2 x nsub)
+  // explicit LES (FP64): jles 1 Smagorinsky, 3 dynamic Smagorinsky
+  int jles = 0;
+  double smagcst = 0.14, maxdsmagcst = 0.3;
+  double* del = nullptr;      // filter width per y row (device, ny)
+  x3d_ctx* cf = nullptr;      // context whose filter has alpha = 0 (dynsmag's filter(zero))
+  double* lw[40] = {nullptr}; // LES work fields
   std::vector<void*> allocs;
   ~SolverImpl() {
     for (void* p : allocs) cudaFree(p);
     if (hpart) cudaFreeHost(hpart);
+    if (cf) x3d_ctx_destroy(cf);
   }
   template <typename T>
   T* alloc(long long n) {
@@ -499,6 +631,139 @@ static int gradp(SolverImpl* s, const T* pp3, T* px, T* py, T* pz, cudaStream_t 
   return X3D_OK;
 }
 
+// ---- explicit LES host side ------------------------------------------------
+// Work-field slots of the LES (FP64, N each)
+enum {
+  LW_P = 0,      // 6: products, filtered, then the Leonard stress L_ij
+  LW_UF = 6,     // 3: filtered velocity
+  LW_T = 9,      // 2: filter ping-pong
+  LW_SF = 11,    // 6: strain of the filtered velocity, then b_ij
+  LW_S = 17,     // 6: strain of the velocity
+  LW_SRT = 23,   // 1: S:S
+  LW_A = 24,     // 6: a_ij, then filtered
+  LW_C = 30,     // 1: dynamic constant
+  LW_NUT = 31,   // 1: eddy viscosity
+  LW_G = 32,     // 3: SGS force
+  LW_D = 35,     // 4: derivatives for the SGS force
+  LW_COUNT = 39
+};
+
+// One dynsmag filter pass (alpha = 0 filter context).
+static int les_fil(SolverImpl* s, int axis, int npaire, double* out, const double* in, cudaStream_t st) {
+  Ctx* f = reinterpret_cast<Ctx*>(s->cf);
+  OpPlan* p = nullptr;
+  int rc = get_plan(f, axis, K_FIL, npaire, default_coefset(K_FIL, npaire), &p);
+  if (rc != X3D_OK) return rc;
+  const int dims[3] = {f->grid.nx, f->grid.ny, f->grid.nz};
+  s->launches++;
+  return launch_line_op<double>(f, p, out, in, dims, nullptr, st, nullptr);
+}
+static int les_fil3(SolverImpl* s, const double* u, int px, int py, int pz, double* out, cudaStream_t st) {
+  double *a = s->lw[LW_T], *b = s->lw[LW_T + 1];
+  RC(les_fil(s, 0, px, a, u, st));
+  RC(les_fil(s, 1, py, b, a, st));
+  return les_fil(s, 2, pz, out, b, st);
+}
+
+// Strain-rate tensor (sxx, syy, szz, sxy, sxz, syz) of smag
+// (src/les_models.f90:190-263); tmp is scratch.
+static int les_strain(SolverImpl* s, const double* ux, const double* uy, const double* uz, double* const* S,
+                      double* tmp, cudaStream_t st) {
+  const int dims[3] = {s->c->grid.nx, s->c->grid.ny, s->c->grid.nz};
+  const double* ppy = ymetric<double>(s, 0);
+  RC(op<double>(s, 0, K_DER1, 0, S[0], ux, dims, st));
+  RC(op<double>(s, 1, K_DER1, 0, S[1], uy, dims, st, nullptr, ppy));
+  RC(op<double>(s, 2, K_DER1, 0, S[2], uz, dims, st));
+  Fuse<double> f = fz_comb<double>(0.5, tmp, 0.5, nullptr, 0.0, nullptr);  // 0.5 (t + tmp), exact halving
+  RC(op<double>(s, 0, K_DER1, 1, tmp, uy, dims, st));                   // gyx
+  RC(op<double>(s, 1, K_DER1, 1, S[3], ux, dims, st, &f, ppy));          // sxy = (gxy + gyx)/2
+  RC(op<double>(s, 2, K_DER1, 1, tmp, ux, dims, st));                   // gxz
+  RC(op<double>(s, 0, K_DER1, 1, S[4], uz, dims, st, &f));               // sxz = (gzx + gxz)/2
+  RC(op<double>(s, 1, K_DER1, 1, tmp, uz, dims, st, nullptr, ppy));      // gzy
+  RC(op<double>(s, 2, K_DER1, 1, S[5], uy, dims, st, &f));               // syz = (gyz + gzy)/2
+  return X3D_OK;
+}
+
+// compute_SGS (src/les_models.f90:96-165, iconserv = 0): eddy viscosity into
+// lw[LW_NUT] and the SGS force into lw[LW_G..LW_G+2].
+static int les_compute(SolverImpl* s, const double* ux, const double* uy, const double* uz, cudaStream_t st) {
+  Ctx* c = s->c;
+  const long long N = s->N;
+  const unsigned nb = pw_blocks(c, N);
+  const int nx = c->grid.nx, ny = c->grid.ny, nz = c->grid.nz;
+  double** w = s->lw;
+  double* S[6] = {w[LW_S], w[LW_S + 1], w[LW_S + 2], w[LW_S + 3], w[LW_S + 4], w[LW_S + 5]};
+  CSix cS = {{S[0], S[1], S[2], S[3], S[4], S[5]}};
+  if (s->jles == 3) {
+    // dynsmag (src/les_models.f90:333-903)
+    double* P[6] = {w[LW_P], w[LW_P + 1], w[LW_P + 2], w[LW_P + 3], w[LW_P + 4], w[LW_P + 5]};
+    k_les_prod<<<nb, 256, 0, st>>>(P[0], P[1], P[2], P[3], P[4], P[5], ux, uy, uz, N);
+    s->launches++;
+    double* uf[3] = {w[LW_UF], w[LW_UF + 1], w[LW_UF + 2]};
+    RC(les_fil3(s, ux, 0, 1, 1, uf[0], st));
+    RC(les_fil3(s, uy, 1, 0, 1, uf[1], st));
+    RC(les_fil3(s, uz, 1, 1, 0, uf[2], st));
+    const int pp[6][3] = {{1, 1, 1}, {1, 1, 1}, {1, 1, 1}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
+    for (int q = 0; q < 6; ++q) RC(les_fil3(s, P[q], pp[q][0], pp[q][1], pp[q][2], P[q], st));
+    k_les_leonard<<<nb, 256, 0, st>>>(Six{{P[0], P[1], P[2], P[3], P[4], P[5]}}, uf[0], uf[1], uf[2], N);
+    s->launches++;
+    double* SF[6] = {w[LW_SF], w[LW_SF + 1], w[LW_SF + 2], w[LW_SF + 3], w[LW_SF + 4], w[LW_SF + 5]};
+    RC(les_strain(s, uf[0], uf[1], uf[2], SF, w[LW_T], st));
+    RC(les_strain(s, ux, uy, uz, S, w[LW_T], st));
+    Six bb = {{SF[0], SF[1], SF[2], SF[3], SF[4], SF[5]}};
+    k_les_tensor<<<nb, 256, 0, st>>>(bb, CSix{{SF[0], SF[1], SF[2], SF[3], SF[4], SF[5]}}, s->del, 2.0, nx, ny, N);
+    double* A[6] = {w[LW_A], w[LW_A + 1], w[LW_A + 2], w[LW_A + 3], w[LW_A + 4], w[LW_A + 5]};
+    k_les_tensor<<<nb, 256, 0, st>>>(Six{{A[0], A[1], A[2], A[3], A[4], A[5]}}, cS, s->del, 1.0, nx, ny, N);
+    k_les_srt<<<nb, 256, 0, st>>>(w[LW_SRT], cS, N);
+    s->launches += 3;
+    for (int q = 0; q < 6; ++q) RC(les_fil3(s, A[q], pp[q][0], pp[q][1], pp[q][2], A[q], st));
+    k_les_smagc<<<nb, 256, 0, st>>>(w[LW_C], CSix{{P[0], P[1], P[2], P[3], P[4], P[5]}},
+                                    CSix{{SF[0], SF[1], SF[2], SF[3], SF[4], SF[5]}},
+                                    CSix{{A[0], A[1], A[2], A[3], A[4], A[5]}}, s->maxdsmagcst, N);
+    s->launches++;
+    RC(les_fil3(s, w[LW_C], 0, 0, 0, w[LW_C], st));
+    k_les_nut_dyn<<<pw_blocks(c, (long long)nx * ny), 256, 0, st>>>(w[LW_NUT], w[LW_C], w[LW_SRT], s->del, nx, ny,
+                                                                     nz);
+    s->launches++;
+  } else {
+    // smag (src/les_models.f90:168-331)
+    RC(les_strain(s, ux, uy, uz, S, w[LW_T], st));
+    k_les_srt<<<nb, 256, 0, st>>>(w[LW_SRT], cS, N);
+    k_les_nut_smag<<<nb, 256, 0, st>>>(w[LW_NUT], w[LW_SRT], s->del, s->smagcst, nx, ny, N);
+    s->launches += 2;
+  }
+  // sgs_mom_nonconservative (src/les_models.f90:1091-1250)
+  const int dims[3] = {nx, ny, nz};
+  double *nut = w[LW_NUT], *gx = w[LW_G], *gy = w[LW_G + 1], *gz = w[LW_G + 2];
+  double *ta = w[LW_D], *td = w[LW_D + 1], *te = w[LW_D + 2], *tf = w[LW_D + 3];
+  const double* ppy = ymetric<double>(s, 0);
+  RC(op<double>(s, 0, K_DER1, 1, ta, nut, dims, st));
+  RC(op<double>(s, 0, K_DER2, 0, td, ux, dims, st));
+  RC(op<double>(s, 0, K_DER2, 1, te, uy, dims, st));
+  RC(op<double>(s, 0, K_DER2, 1, tf, uz, dims, st));
+  k_les_sgs<<<nb, 256, 0, st>>>(gx, gy, gz, td, te, tf, nut, ta, S[0], S[3], S[4], 1, N);
+  RC(op<double>(s, 1, K_DER1, 1, ta, nut, dims, st, nullptr, ppy));
+  const double* us[3] = {ux, uy, uz};
+  double* ts[3] = {td, te, tf};
+  const int par[3] = {1, 0, 1};
+  for (int q = 0; q < 3; ++q) {
+    RC(op<double>(s, 1, K_DER2, par[q], ts[q], us[q], dims, st));
+    if (ppy) {
+      RC(op<double>(s, 1, K_DER1, par[q], w[LW_T], us[q], dims, st, nullptr, ppy));
+      k_stretch_d2<<<nb, 256, 0, st>>>(ts[q], w[LW_T], ymetric<double>(s, 1), ymetric<double>(s, 2), nx, ny, N);
+      s->launches++;
+    }
+  }
+  k_les_sgs<<<nb, 256, 0, st>>>(gx, gy, gz, td, te, tf, nut, ta, S[3], S[1], S[5], 0, N);
+  RC(op<double>(s, 2, K_DER1, 1, ta, nut, dims, st));
+  RC(op<double>(s, 2, K_DER2, 1, td, ux, dims, st));
+  RC(op<double>(s, 2, K_DER2, 1, te, uy, dims, st));
+  RC(op<double>(s, 2, K_DER2, 0, tf, uz, dims, st));
+  k_les_sgs<<<nb, 256, 0, st>>>(gx, gy, gz, td, te, tf, nut, ta, S[4], S[5], S[2], 0, N);
+  s->launches += 3;
+  return cuda_status(cudaGetLastError());
+}
+
 // ppy as channel_cfr divides by it: the stretching metric, or on a uniform
 // mesh the default 1 with 2 at the walls (src/variables.f90:1294-1305).
 static const double* ymetric_cfr(SolverImpl* s) {
@@ -528,6 +793,13 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
     s->launches += 3;
   }
   RC(momentum_rhs<T>(s, u, H, st));
+  if (s->jles != 0) {
+    // src/transeq.f90:475-480: the SGS force joins the right-hand side
+    RC(les_compute(s, s->ux, s->uy, s->uz, st));
+    k_add3<<<nb, 256, 0, st>>>((double*)H[0], (double*)H[1], (double*)H[2], s->lw[LW_G], s->lw[LW_G + 1],
+                               s->lw[LW_G + 2], N);
+    s->launches++;
+  }
   if (s->walls && s->wrotation != 0.0 && it < s->spinup_time) {
     k_rotation<<<nb, 256, 0, st>>>((double*)H[0], (double*)H[1], s->ux, s->uy, s->wrotation, N);
     s->launches++;
@@ -722,6 +994,56 @@ int x3d_solver_set_channel(x3d_solver* s, double target_ub, double wrotation, in
   si->cfr_target = target_ub;
   si->wrotation = wrotation;
   si->spinup_time = spinup_time;
+  return X3D_OK;
+}
+
+int x3d_solver_set_les(x3d_solver* s, int jles, double smagcst, double maxdsmagcst) {
+  if (!s) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  if (jles != 0 && jles != 1 && jles != 3) return X3D_ERR_UNSUPPORTED;
+  if (si->mixed()) return X3D_ERR_DTYPE;
+  Ctx* c = si->c;
+  if (jles != 0 && !si->lw[0]) {
+    // filter width del(j) of init_explicit_les (src/les_models.f90:27-30)
+    const int ny = c->grid.ny;
+    std::vector<double> del(ny);
+    for (int j = 0; j < ny - 1; ++j)
+      del[j] = std::pow(c->ax[0].d * (c->st.yp[j + 1] - c->st.yp[j]) * c->ax[2].d, 1.0 / 3.0);
+    del[ny - 1] = del[ny - 2];
+    si->del = si->alloc<double>(ny);
+    if (!si->del) return X3D_ERR_NOMEM;
+    int rc = cuda_status(cudaMemcpy(si->del, del.data(), ny * sizeof(double), cudaMemcpyHostToDevice));
+    if (rc != X3D_OK) return rc;
+    // dynsmag filters with alpha = 0 (filter(zero), src/les_models.f90:393)
+    x3d_numopts o = c->opts;
+    o.filter_alpha = 0.0;
+    rc = x3d_ctx_create(&c->grid, &o, &si->cf);
+    if (rc != X3D_OK) return rc;
+    for (int k = 0; k < LW_COUNT; ++k) {
+      si->lw[k] = si->alloc<double>(si->N);
+      if (!si->lw[k]) return X3D_ERR_NOMEM;
+    }
+  }
+  si->jles = jles;
+  si->smagcst = smagcst;
+  si->maxdsmagcst = maxdsmagcst;
+  return X3D_OK;
+}
+
+int x3d_solver_les_fields(x3d_solver* s, double* nut, double* sgsx, double* sgsy, double* sgsz, void* stream) {
+  if (!s || !nut || !sgsx || !sgsy || !sgsz) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  if (si->jles == 0) return X3D_ERR_STATE;
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = les_compute(si, si->ux, si->uy, si->uz, st);
+  if (rc != X3D_OK) return rc;
+  const size_t b = (size_t)si->N * sizeof(double);
+  double* dst[4] = {nut, sgsx, sgsy, sgsz};
+  const double* src[4] = {si->lw[LW_NUT], si->lw[LW_G], si->lw[LW_G + 1], si->lw[LW_G + 2]};
+  for (int q = 0; q < 4; ++q) {
+    rc = cuda_status(cudaMemcpyAsync(dst[q], src[q], b, cudaMemcpyDeviceToDevice, st));
+    if (rc != X3D_OK) return rc;
+  }
   return X3D_OK;
 }
 

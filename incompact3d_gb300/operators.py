@@ -277,6 +277,18 @@ class Solver:
         check(self.lib.x3d_solver_set_channel(self.h, target_ub, wrotation, spinup_time),
               "x3d_solver_set_channel")
 
+    def set_les(self, jles, smagcst=0.14, maxdsmagcst=0.3):
+        """Explicit LES model: 1 Smagorinsky, 3 dynamic Smagorinsky, 0 off."""
+        check(self.lib.x3d_solver_set_les(self.h, jles, smagcst, maxdsmagcst), "x3d_solver_set_les")
+
+    def les_fields(self):
+        """(nut, sgsx, sgsy, sgsz) of the current velocity, as CUDA tensors."""
+        torch = _torch()
+        nx, ny, nz = self.ctx.n
+        out = [torch.empty((nz, ny, nx), dtype=torch.float64, device="cuda") for _ in range(4)]
+        check(self.lib.x3d_solver_les_fields(self.h, *[_ptr(o) for o in out], _stream()), "x3d_solver_les_fields")
+        return out
+
     def bulk_velocity(self):
         """Bulk velocity seen by the flow-rate control at each sub-step of the last step."""
         out = np.zeros(8)

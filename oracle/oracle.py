@@ -56,6 +56,8 @@ def _load():
             lib.ox_run.argtypes = [P, D, D, D, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_int, ctypes.c_int, D, D]
             lib.ox_stretching.argtypes = [P, ctypes.c_int, D]
+            lib.ox_set_les.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+            lib.ox_les.argtypes = [P, D, D, D, D, D, D, D]
             lib.ox_run_channel.argtypes = [P, D, D, D, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_int, ctypes.c_double, ctypes.c_int, D, D]
             _lib = lib
@@ -194,3 +196,15 @@ class Oracle:
                                     wrotation, spinup_time, _dp(ub), _dp(dmax))
         assert n >= 0, n
         return ux, uy, uz, ub[:n], float(dmax[0])
+
+    def set_les(self, jles, smagcst=0.14, maxdsmagcst=0.3):
+        """Explicit LES model in the right-hand side: 1 Smagorinsky, 3 dynamic."""
+        assert self.lib.ox_set_les(self.h, jles, smagcst, maxdsmagcst) == 0
+
+    def les(self, ux, uy, uz):
+        """(nut, sgsx, sgsy, sgsz) of compute_SGS for the current model."""
+        shp = (self.nz, self.ny, self.nx)
+        out = [np.empty(shp) for _ in range(4)]
+        rc = self.lib.ox_les(self.h, _dp(_c64(ux)), _dp(_c64(uy)), _dp(_c64(uz)), *[_dp(o) for o in out])
+        assert rc == 0, rc
+        return out

@@ -747,6 +747,11 @@ struct OxCtx {
   vec sax, sbx, say, sby, saz, sbz;
   // poisson_010 tables (x, z periodic; y non-periodic on nym points)
   vec yky10, yk210, eys10, trx10, try10, trz10;
+  // explicit LES (src/les_models.f90): jles 0 none, 1 Smagorinsky, 3 dynamic
+  int jles = 0;
+  double smagcst = 0.14, maxdsmagcst = 0.3;
+  vec del;      // filter width per y row (init_explicit_les)
+  Axis axf[3];  // the axes with filter coefficients of alpha = 0 (dynsmag's filter(zero))
 };
 
 namespace {
@@ -936,8 +941,8 @@ void abxyz_half(int n, vec& sa, vec& sb) {
 // Apply operator `op` along `axis` to the 3-D field u (dims nin along the axis),
 // writing t (dims nout along the axis).  dims[] are the input dims.
 void apply3d(const OxCtx& c, int axis, int op, int npaire, const double* u, double* t, const int dims[3],
-             const double* pp) {
-  const Axis& a = c.ax[axis];
+             const double* pp, const Axis* override_axis = nullptr) {
+  const Axis& a = override_axis ? *override_axis : c.ax[axis];
   const OpPlan p = plan_op(a, op, npaire);
   int din[3] = {dims[0], dims[1], dims[2]};
   int dout[3] = {dims[0], dims[1], dims[2]};
@@ -1395,6 +1400,217 @@ static void poisson_010(const OxCtx& c, double* rhs) {
 }
 
 // ---------------------------------------------------------------------------
+// Explicit LES: src/les_models.f90
+// ---------------------------------------------------------------------------
+struct StrainT {
+  vec sxx, syy, szz, sxy, sxz, syz, srt;
+};
+
+// Strain-rate tensor and srt = S:S of smag (src/les_models.f90:168-270).
+static void les_strain(const OxCtx& c, const vec& ux, const vec& uy, const vec& uz, StrainT& S) {
+  const size_t N = ux.size();
+  const int dims[3] = {c.nx, c.ny, c.nz};
+  const double* ppy = (c.istret != 0) ? c.ppy.data() : nullptr;
+  vec gxx(N), gyx(N), gzx(N), gxy(N), gyy(N), gzy(N), gxz(N), gyz(N), gzz(N);
+  apply3d(c, 0, OP_DER1, 0, ux.data(), gxx.data(), dims, nullptr);
+  apply3d(c, 0, OP_DER1, 1, uy.data(), gyx.data(), dims, nullptr);
+  apply3d(c, 0, OP_DER1, 1, uz.data(), gzx.data(), dims, nullptr);
+  apply3d(c, 1, OP_DER1, 1, ux.data(), gxy.data(), dims, ppy);
+  apply3d(c, 1, OP_DER1, 0, uy.data(), gyy.data(), dims, ppy);
+  apply3d(c, 1, OP_DER1, 1, uz.data(), gzy.data(), dims, ppy);
+  apply3d(c, 2, OP_DER1, 1, ux.data(), gxz.data(), dims, nullptr);
+  apply3d(c, 2, OP_DER1, 1, uy.data(), gyz.data(), dims, nullptr);
+  apply3d(c, 2, OP_DER1, 0, uz.data(), gzz.data(), dims, nullptr);
+  S.sxx = gxx; S.syy = gyy; S.szz = gzz;
+  S.sxy.resize(N); S.syz.resize(N); S.sxz.resize(N); S.srt.resize(N);
+  for (size_t m = 0; m < N; ++m) {
+    S.sxy[m] = 0.5 * (gxy[m] + gyx[m]);
+    S.syz[m] = 0.5 * (gyz[m] + gzy[m]);
+    S.sxz[m] = 0.5 * (gzx[m] + gxz[m]);
+  }
+  for (size_t m = 0; m < N; ++m)
+    S.srt[m] = S.sxx[m] * S.sxx[m] + S.syy[m] * S.syy[m] + S.szz[m] * S.szz[m] + 2.0 * S.sxy[m] * S.sxy[m] +
+               2.0 * S.sxz[m] * S.sxz[m] + 2.0 * S.syz[m] * S.syz[m];
+}
+
+inline int jrow(size_t m, int nx, int ny) { return (int)((m / (size_t)nx) % (size_t)ny); }
+
+// smag (src/les_models.f90:168-331), itype != abl: nut = (Cs del)^2 sqrt(2 S:S).
+static void les_smag(const OxCtx& c, const StrainT& S, vec& nut) {
+  const size_t N = S.srt.size();
+  nut.assign(N, 0.0);
+  for (size_t m = 0; m < N; ++m) {
+    const double length = c.smagcst * c.del[jrow(m, c.nx, c.ny)];
+    nut[m] = (length * length) * std::sqrt(2.0 * S.srt[m]);
+  }
+}
+
+// One filter pass of dynsmag (filx / fily / filz with the alpha = 0 filter).
+static void les_fil(const OxCtx& c, int axis, int npaire, const vec& u, vec& t) {
+  const int dims[3] = {c.nx, c.ny, c.nz};
+  t.resize(u.size());
+  apply3d(c, axis, OP_FIL, npaire, u.data(), t.data(), dims, nullptr, &c.axf[axis]);
+}
+// x, then y, then z filtering with one parity per direction.
+static void les_fil3(const OxCtx& c, const vec& u, int px, int py, int pz, vec& out) {
+  vec a, b;
+  les_fil(c, 0, px, u, a);
+  les_fil(c, 1, py, a, b);
+  les_fil(c, 2, pz, b, out);
+}
+
+// dynsmag (src/les_models.f90:333-903), no IBM.  Returns nut; S receives the
+// strain tensor of the unfiltered velocity (used by the SGS divergence).
+static void les_dynsmag(const OxCtx& c, const vec& ux, const vec& uy, const vec& uz, vec& nut, StrainT& S) {
+  const size_t N = ux.size();
+  vec uxx(N), uyy(N), uzz(N), uxy(N), uxz(N), uyz(N);
+  for (size_t m = 0; m < N; ++m) {
+    uxx[m] = ux[m] * ux[m]; uyy[m] = uy[m] * uy[m]; uzz[m] = uz[m] * uz[m];
+    uxy[m] = ux[m] * uy[m]; uxz[m] = ux[m] * uz[m]; uyz[m] = uy[m] * uz[m];
+  }
+  vec uxf, uyf, uzf, uxxf, uyyf, uzzf, uxyf, uxzf, uyzf;
+  les_fil3(c, ux, 0, 1, 1, uxf);
+  les_fil3(c, uy, 1, 0, 1, uyf);
+  les_fil3(c, uz, 1, 1, 0, uzf);
+  les_fil3(c, uxx, 1, 1, 1, uxxf);
+  les_fil3(c, uyy, 1, 1, 1, uyyf);
+  les_fil3(c, uzz, 1, 1, 1, uzzf);
+  les_fil3(c, uxy, 0, 0, 1, uxyf);
+  les_fil3(c, uxz, 0, 1, 0, uxzf);
+  les_fil3(c, uyz, 1, 0, 0, uyzf);
+  vec lxx(N), lyy(N), lzz(N), lxy(N), lxz(N), lyz(N);
+  for (size_t m = 0; m < N; ++m) {
+    lxx[m] = uxxf[m] - uxf[m] * uxf[m];
+    lyy[m] = uyyf[m] - uyf[m] * uyf[m];
+    lzz[m] = uzzf[m] - uzf[m] * uzf[m];
+    lxy[m] = uxyf[m] - uxf[m] * uyf[m];
+    lxz[m] = uxzf[m] - uxf[m] * uzf[m];
+    lyz[m] = uyzf[m] - uyf[m] * uzf[m];
+  }
+  StrainT Sf;
+  les_strain(c, uxf, uyf, uzf, Sf);
+  les_strain(c, ux, uy, uz, S);
+  vec bb[6], aa[6];
+  const vec* sf[6] = {&Sf.sxx, &Sf.syy, &Sf.szz, &Sf.sxy, &Sf.sxz, &Sf.syz};
+  const vec* su[6] = {&S.sxx, &S.syy, &S.szz, &S.sxy, &S.sxz, &S.syz};
+  for (int q = 0; q < 6; ++q) { bb[q].resize(N); aa[q].resize(N); }
+  for (size_t m = 0; m < N; ++m) {
+    const double mf = std::sqrt(2.0 * (Sf.sxx[m] * Sf.sxx[m] + Sf.syy[m] * Sf.syy[m] + Sf.szz[m] * Sf.szz[m] +
+                                       2.0 * Sf.sxy[m] * Sf.sxy[m] + 2.0 * Sf.sxz[m] * Sf.sxz[m] +
+                                       2.0 * Sf.syz[m] * Sf.syz[m]));
+    const double mu = std::sqrt(2.0 * (S.sxx[m] * S.sxx[m] + S.syy[m] * S.syy[m] + S.szz[m] * S.szz[m] +
+                                       2.0 * S.sxy[m] * S.sxy[m] + 2.0 * S.sxz[m] * S.sxz[m] +
+                                       2.0 * S.syz[m] * S.syz[m]));
+    const double dl = c.del[jrow(m, c.nx, c.ny)];
+    for (int q = 0; q < 6; ++q) {
+      bb[q][m] = -2.0 * mf * (*sf[q])[m];
+      aa[q][m] = -2.0 * mu * (*su[q])[m];
+      aa[q][m] = aa[q][m] * (dl * dl);
+      bb[q][m] = bb[q][m] * ((2.0 * dl) * (2.0 * dl));
+    }
+  }
+  // filtered a_ij (parities per direction: src/les_models.f90:681-779)
+  const int pa[6][3] = {{1, 1, 1}, {1, 1, 1}, {1, 1, 1}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
+  vec af[6];
+  for (int q = 0; q < 6; ++q) les_fil3(c, aa[q], pa[q][0], pa[q][1], pa[q][2], af[q]);
+  vec smagC(N);
+  for (size_t m = 0; m < N; ++m) {
+    const double mxx = bb[0][m] - af[0][m], myy = bb[1][m] - af[1][m], mzz = bb[2][m] - af[2][m];
+    const double mxy = bb[3][m] - af[3][m], mxz = bb[4][m] - af[4][m], myz = bb[5][m] - af[5][m];
+    // deviatoric part, statement by statement as the reference writes it
+    lxx[m] = lxx[m] - (lxx[m] + lyy[m] + lzz[m]) / 3.0;
+    lyy[m] = lyy[m] - (lxx[m] + lyy[m] + lzz[m]) / 3.0;
+    lzz[m] = lzz[m] - (lxx[m] + lyy[m] + lzz[m]) / 3.0;
+    double v = (lxx[m] * mxx + lyy[m] * myy + lzz[m] * mzz + 2.0 * (lxy[m] * mxy + lxz[m] * mxz + lyz[m] * myz)) /
+               (mxx * mxx + myy * myy + mzz * mzz + 2.0 * (mxy * mxy + mxz * mxz + myz * myz));
+    if (v > c.maxdsmagcst) v = c.maxdsmagcst;
+    if (v < 0.0) v = 0.0;
+    smagC[m] = v;
+  }
+  vec cf;
+  les_fil3(c, smagC, 0, 0, 0, cf);
+  // mean over z (tools.f90 mean_plane_z), broadcast along z
+  const int nx = c.nx, ny = c.ny, nz = c.nz;
+  vec cm((size_t)nx * ny, 0.0);
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) {
+      double sum = 0.0;
+      for (int k = 0; k < nz; ++k) sum = sum + cf[idx3(i, j, k, nx, ny)];
+      cm[(size_t)i + (size_t)nx * j] = sum / (double)nz;
+    }
+  nut.assign(N, 0.0);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const size_t m = idx3(i, j, k, nx, ny);
+        const double dl = c.del[j];
+        nut[m] = cm[(size_t)i + (size_t)nx * j] * (dl * dl) * std::sqrt(2.0 * S.srt[m]);
+      }
+}
+
+// sgs_mom_nonconservative (src/les_models.f90:1091-1250), no IBM.
+static void les_sgs(const OxCtx& c, const vec& ux, const vec& uy, const vec& uz, const vec& nut, const StrainT& S,
+                    vec& gx, vec& gy, vec& gz) {
+  const size_t N = ux.size();
+  const int dims[3] = {c.nx, c.ny, c.nz};
+  const double* ppy = (c.istret != 0) ? c.ppy.data() : nullptr;
+  vec ta(N), td(N), te(N), tf(N), tj(N);
+  gx.assign(N, 0.0); gy.assign(N, 0.0); gz.assign(N, 0.0);
+  apply3d(c, 0, OP_DER1, 1, nut.data(), ta.data(), dims, nullptr);
+  apply3d(c, 0, OP_DER2, 0, ux.data(), td.data(), dims, nullptr);
+  apply3d(c, 0, OP_DER2, 1, uy.data(), te.data(), dims, nullptr);
+  apply3d(c, 0, OP_DER2, 1, uz.data(), tf.data(), dims, nullptr);
+  for (size_t m = 0; m < N; ++m) {
+    gx[m] = td[m] * nut[m] + 2.0 * S.sxx[m] * ta[m];
+    gy[m] = te[m] * nut[m] + 2.0 * S.sxy[m] * ta[m];
+    gz[m] = tf[m] * nut[m] + 2.0 * S.sxz[m] * ta[m];
+  }
+  apply3d(c, 1, OP_DER1, 1, nut.data(), ta.data(), dims, ppy);
+  const vec* us[3] = {&ux, &uy, &uz};
+  vec* ts[3] = {&td, &te, &tf};
+  const int par[3] = {1, 0, 1};
+  for (int q = 0; q < 3; ++q) {
+    apply3d(c, 1, OP_DER2, par[q], us[q]->data(), ts[q]->data(), dims, nullptr);
+    if (c.istret != 0) {
+      apply3d(c, 1, OP_DER1, par[q], us[q]->data(), tj.data(), dims, c.ppy.data());
+      vec& t = *ts[q];
+      for (size_t m = 0; m < N; ++m) {
+        const int j = jrow(m, c.nx, c.ny);
+        t[m] = t[m] * c.pp2y[j] - c.pp4y[j] * tj[m];
+      }
+    }
+  }
+  for (size_t m = 0; m < N; ++m) {
+    gx[m] = gx[m] + nut[m] * td[m] + 2.0 * S.sxy[m] * ta[m];
+    gy[m] = gy[m] + nut[m] * te[m] + 2.0 * S.syy[m] * ta[m];
+    gz[m] = gz[m] + nut[m] * tf[m] + 2.0 * S.syz[m] * ta[m];
+  }
+  apply3d(c, 2, OP_DER1, 1, nut.data(), ta.data(), dims, nullptr);
+  apply3d(c, 2, OP_DER2, 1, ux.data(), td.data(), dims, nullptr);
+  apply3d(c, 2, OP_DER2, 1, uy.data(), te.data(), dims, nullptr);
+  apply3d(c, 2, OP_DER2, 0, uz.data(), tf.data(), dims, nullptr);
+  for (size_t m = 0; m < N; ++m) {
+    gx[m] = gx[m] + nut[m] * td[m] + 2.0 * S.sxz[m] * ta[m];
+    gy[m] = gy[m] + nut[m] * te[m] + 2.0 * S.syz[m] * ta[m];
+    gz[m] = gz[m] + nut[m] * tf[m] + 2.0 * S.szz[m] * ta[m];
+  }
+}
+
+// compute_SGS (src/les_models.f90:96-165), iconserv = 0: eddy viscosity and
+// the SGS force.
+static void les_compute(const OxCtx& c, const vec& ux, const vec& uy, const vec& uz, vec& nut, vec& gx, vec& gy,
+                        vec& gz) {
+  StrainT S;
+  if (c.jles == 1) {
+    les_strain(c, ux, uy, uz, S);
+    les_smag(c, S, nut);
+  } else {
+    les_dynsmag(c, ux, uy, uz, nut, S);
+  }
+  les_sgs(c, ux, uy, uz, nut, S, gx, gy, gz);
+}
+
+// ---------------------------------------------------------------------------
 // Incompressible step for the plain periodic case
 // ---------------------------------------------------------------------------
 struct Fields {
@@ -1509,6 +1725,16 @@ static void momentum_rhs(const OxCtx& c, const vec& ux, const vec& uy, const vec
     hx[m] = ta2[m] - 0.5 * tg1[m] + td[m];
     hy[m] = tb2[m] - 0.5 * th1[m] + te[m];
     hz[m] = tc2[m] - 0.5 * ti1[m] + tf[m];
+  }
+  if (c.jles == 1 || c.jles == 3) {
+    // src/transeq.f90:475-480: dux1 += sgsx1, ...
+    vec nut, gx, gy, gz;
+    les_compute(c, ux, uy, uz, nut, gx, gy, gz);
+    for (size_t m = 0; m < N; ++m) {
+      hx[m] = hx[m] + gx[m];
+      hy[m] = hy[m] + gy[m];
+      hz[m] = hz[m] + gz[m];
+    }
   }
 }
 
@@ -1660,6 +1886,43 @@ int ox_poisson(void* h, double* rhs) {
     return 0;
   }
   return -2;
+}
+
+// Explicit LES model for the right-hand side (src/les_models.f90):
+// jles 0 none, 1 Smagorinsky, 3 dynamic Smagorinsky.  Sets the filter width
+// del(j) of init_explicit_les (src/les_models.f90:27-30) and the alpha = 0
+// filter dynsmag uses (filter(zero), src/les_models.f90:393).
+int ox_set_les(void* h, int jles, double smagcst, double maxdsmagcst) {
+  OxCtx* c = (OxCtx*)h;
+  if (jles != 0 && jles != 1 && jles != 3) return -1;
+  c->jles = jles;
+  c->smagcst = smagcst;
+  c->maxdsmagcst = maxdsmagcst;
+  const int ny = c->ny;
+  c->del.assign(ny, 0.0);
+  for (int j = 0; j < ny - 1; ++j)
+    c->del[j] = std::pow(c->ax[0].d * (c->yp[j + 1] - c->yp[j]) * c->ax[2].d, 1.0 / 3.0);
+  c->del[ny - 1] = c->del[ny - 2];
+  for (int a = 0; a < 3; ++a) {
+    c->axf[a] = c->ax[a];
+    filter_coefficients(c->axf[a], 0.0);
+  }
+  return 0;
+}
+
+// Eddy viscosity and SGS force of compute_SGS for the current LES model.
+int ox_les(void* h, const double* ux, const double* uy, const double* uz, double* nut, double* gx, double* gy,
+           double* gz) {
+  const OxCtx* c = (const OxCtx*)h;
+  if (c->jles != 1 && c->jles != 3) return -1;
+  const size_t N = (size_t)c->nx * c->ny * c->nz;
+  vec a(ux, ux + N), b(uy, uy + N), d(uz, uz + N), n, x, y, z;
+  les_compute(*c, a, b, d, n, x, y, z);
+  std::memcpy(nut, n.data(), N * sizeof(double));
+  std::memcpy(gx, x.data(), N * sizeof(double));
+  std::memcpy(gy, y.data(), N * sizeof(double));
+  std::memcpy(gz, z.data(), N * sizeof(double));
+  return 0;
 }
 
 // Stretching metrics: which = 0..7 -> yp, ypi, ppy, pp2y, pp4y, ppyi, pp2yi,
