@@ -10,6 +10,7 @@ with the kinetic-energy difference between the two after the same steps.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--n 512] [--impl ours|reference]
   python bench.py --workload ops [--n 512] [--ops dery,...] [--dtypes f64,f32] [--bcs 0,2]
   python bench.py --workload channel [--steps K] [--warmup W]
+  python bench.py --workload les [--steps K] [--warmup W]
 
 --impl reference times the CPU restatement of the reference's path (the
 parity oracle, C++/OpenMP on all host cores) on a bounded sample grid of the
@@ -358,7 +359,10 @@ def run_ops(args):
         ctx = x3d.Context(n, n, n, L, L, L)
         rhs0 = spectral_field(torch, n, L, True, zero_mean=True)
         rhs = torch.empty_like(rhs0)
+        arith = set(args.poisson_arith.split(","))
         for prec, nm in ((0, "fp64"), (2, "double-float"), (1, "fp32")):
+            if nm not in arith:
+                continue
             def solve():
                 rhs.copy_(rhs0)
                 ctx.poisson(rhs, precision=prec)
@@ -430,15 +434,47 @@ def run_channel(args):
     print(json.dumps(line), flush=True)
 
 
+def run_les(args):
+    """LES of the TGV at Re=5000 on 128^3 (FP64, AB3, dt=0.005): the
+    dynamic-Smagorinsky step and the Smagorinsky step timed beside the plain
+    (no-model) step; the ratio is the SGS model's cost factor."""
+    import numpy as np
+    import torch
+    import incompact3d_gb300 as x3d
+
+    x3d.build()
+    n = 128
+    L = 2 * np.pi
+    ctx = x3d.Context(n, n, n, L, L, L)
+    stream = torch.cuda.current_stream()
+    out = {"workload": "tgv_les_128^3_re5000_ab3_fp64", "metric": "LES step Mpts*steps/s", "unit": UNIT,
+           "dtype": "f64", "steps": args.steps, "warmup": args.warmup}
+    for name, jles in (("plain", 0), ("smag", 1), ("dynsmag", 3)):
+        s = x3d.Solver(ctx, 0.005, 1 / 5000.0, itimescheme=3, precision=x3d.PREC_FP64)
+        if jles:
+            s.set_les(jles, 0.14, 0.3)
+        s.init_tgv()
+        s.step(args.warmup)
+        secs = time_steps(torch, s, args.steps, stream)
+        out[name] = {"ms_per_step": round(1e3 * secs / args.steps, 3),
+                     "value": round(n ** 3 * args.steps / secs / 1e6, 3),
+                     "launches_per_step": s.lib.x3d_solver_launches_per_step(s.h)}
+        s.close()
+    out["value"] = out["dynsmag"]["value"]
+    out["dynsmag_over_plain"] = round(out["dynsmag"]["ms_per_step"] / out["plain"]["ms_per_step"], 3)
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "ops", "channel"],
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "ops", "channel", "les"],
                     help="tgv: the time-step benchmark (default); ops: operator microbench lines; "
                          "channel: the stretched turbulent channel (FP64)")
     ap.add_argument("--ops", default="", help="ops workload: comma list (derx,...,filz,poisson)")
     ap.add_argument("--dtypes", default="f64,f32")
     ap.add_argument("--bcs", default="0,2")
     ap.add_argument("--reps", type=int, default=10)
+    ap.add_argument("--poisson-arith", default="fp64,double-float,fp32")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
@@ -457,6 +493,8 @@ def main():
         run_ops(args)
     elif args.workload == "channel":
         run_channel(args)
+    elif args.workload == "les":
+        run_les(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -21,6 +21,8 @@ Ctx::~Ctx() {
   }
   if (st.d_ppy) cudaFree(st.d_ppy);
   if (d_p010) cudaFree(d_p010);
+  for (void* t : d_inv)
+    if (t) cudaFree(t);
   if (d_twid) cudaFree(d_twid);
   if (d_twid32) cudaFree(d_twid32);
   if (d_twid_df) cudaFree(d_twid_df);

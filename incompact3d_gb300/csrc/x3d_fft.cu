@@ -234,11 +234,19 @@ __device__ __forceinline__ void stockham_pass(C* buf, int lstride, int n, int nl
 
 template <int SIGN, typename P, typename C>
 __device__ void smem_fft(C* buf, int lstride, int n, int nl, const C* tw) {
+  // nl * n <= FFT_ELEMS: one radix group of FFT_VALS values per thread
   int Ns = 1;
   int rem = n;
   while (rem >= 8) { stockham_pass<8, SIGN, P>(buf, lstride, n, nl, Ns, tw); Ns *= 8; rem /= 8; }
   if (rem == 4) { stockham_pass<4, SIGN, P>(buf, lstride, n, nl, Ns, tw); Ns *= 4; rem /= 4; }
   if (rem == 2) { stockham_pass<2, SIGN, P>(buf, lstride, n, nl, Ns, tw); }
+}
+
+// Lines per CTA of a strided pass: one radix group of values per thread
+// (wider CTAs with fewer resident per SM measured slower at 512^3).
+template <typename C>
+int strided_lanes(int n) {
+  return std::max(1, std::min(32, FFT_ELEMS / n));
 }
 
 // ---- Pass A: x real-to-complex --------------------------------------------
@@ -316,6 +324,9 @@ struct Spec {
   const float2* trdf[3];
   int nx, ny, nz;
   double scale;  // 1/(nx*ny*nz)
+  // optional per-mode factor -scale/K (0 where K < 1e-16), layout of the
+  // spectrum, in the policy's number format (double, float, hi/lo float2)
+  const void* inv;
 };
 
 // K of poisson_000's kxyz (src/poisson.f90:1688-1724, periodic): unfused IEEE
@@ -361,6 +372,55 @@ struct Spectral<DF> {
   }
 };
 
+// Multiply a mode by its tabulated factor.
+template <typename P>
+struct InvMul;
+template <>
+struct InvMul<double> {
+  static __device__ __forceinline__ double2 mul(double2 v, const void* t, long long i) {
+    const double f = reinterpret_cast<const double*>(t)[i];
+    return make_double2(v.x * f, v.y * f);
+  }
+};
+template <>
+struct InvMul<float> {
+  static __device__ __forceinline__ float2 mul(float2 v, const void* t, long long i) {
+    const float f = reinterpret_cast<const float*>(t)[i];
+    return make_float2(v.x * f, v.y * f);
+  }
+};
+template <>
+struct InvMul<DF> {
+  static __device__ __forceinline__ cdf mul(cdf v, const void* t, long long i) {
+    const float2 f2 = reinterpret_cast<const float2*>(t)[i];
+    const df f{f2.x, f2.y};
+    return FT<DF>::mk(df_mul(FT<DF>::R_(v), f), df_mul(FT<DF>::I_(v), f));
+  }
+};
+
+// Per-mode factor table -scale/K of poisson_000 (K and the zeroing rule as in
+// kxyz64), built once per context and number format.
+template <typename P>
+__global__ void k_inv_table(void* out, Spec sp) {
+  const int nxh = sp.nx / 2 + 1;
+  const long long n = (long long)nxh * sp.ny * sp.nz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(i % nxh);
+    const int ky = (int)((i / nxh) % sp.ny);
+    const int kz = (int)(i / ((long long)nxh * sp.ny));
+    const double kk = kxyz64(sp, kx, ky, kz);
+    const double f = (kk < 1.0e-16) ? 0.0 : -sp.scale / kk;
+    if (std::is_same<P, double>::value) {
+      reinterpret_cast<double*>(out)[i] = f;
+    } else if (std::is_same<P, float>::value) {
+      reinterpret_cast<float*>(out)[i] = (float)f;
+    } else {
+      const float h = (float)f;
+      reinterpret_cast<float2*>(out)[i] = make_float2(h, (float)(f - (double)h));
+    }
+  }
+}
+
 template <typename P, bool POISSON, int SIGN>
 __global__ void __launch_bounds__(FFT_THREADS) fft_strided(typename Cx<P>::T* __restrict__ data, int n, long long rs,
                                                            int na, int lanes, long long bs,
@@ -382,9 +442,18 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_strided(typename Cx<P>::T* __
   smem_fft<SIGN, P>(buf, lstride, n, nl, SIGN < 0 ? tw_f : tw_i);
   if (POISSON) {
     // z-lines: a = kx (0..nx/2), b = ky; row r = kz
-    for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
-      const int l = e / n, kz = e - l * n;
-      buf[l * lstride + kz] = Spectral<P>::apply(buf[l * lstride + kz], sp, a0 + l, (int)b, kz);
+    if (sp.inv) {
+      const int nxh = sp.nx / 2 + 1;
+      for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
+        const int l = e / n, kz = e - l * n;
+        const long long i = ((long long)kz * sp.ny + b) * nxh + a0 + l;
+        buf[l * lstride + kz] = InvMul<P>::mul(buf[l * lstride + kz], sp.inv, i);
+      }
+    } else {
+      for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
+        const int l = e / n, kz = e - l * n;
+        buf[l * lstride + kz] = Spectral<P>::apply(buf[l * lstride + kz], sp, a0 + l, (int)b, kz);
+      }
     }
     __syncthreads();
     smem_fft<1, P>(buf, lstride, n, nl, tw_i);
@@ -503,6 +572,19 @@ static int poisson_run(Ctx* c, double* rhs, cudaStream_t st) {
   }
   sp.nx = nx; sp.ny = ny; sp.nz = nz;
   sp.scale = 1.0 / ((double)nx * (double)ny * (double)nz);
+  sp.inv = nullptr;
+  {
+    // per-mode factor table, built on first use for this number format
+    const int slot = std::is_same<R, double>::value ? 0 : std::is_same<R, float>::value ? 1 : 2;
+    if (!c->d_inv[slot]) {
+      const size_t es = slot == 1 ? sizeof(float) : sizeof(double);
+      void* t = nullptr;
+      if (cudaMalloc(&t, (size_t)nxh * ny * nz * es) != cudaSuccess) return X3D_ERR_NOMEM;
+      k_inv_table<R><<<4 * c->num_sms, 256, 0, st>>>(t, sp);
+      c->d_inv[slot] = t;
+    }
+    sp.inv = c->d_inv[slot];
+  }
 
   // A: x r2c
   {
@@ -515,7 +597,7 @@ static int poisson_run(Ctx* c, double* rhs, cudaStream_t st) {
     k<<<nb, FFT_THREADS, smem, st>>>(rhs, spec, nx, nlines, lpb, twx_f, twx_full);
   }
   // B: y forward, lines over kx with stride nxh, outer over z
-  const int lanes_y = std::max(1, std::min(32, FFT_ELEMS / ny));
+  const int lanes_y = strided_lanes<C>(ny);
   const size_t smem_y = (size_t)lanes_y * (ny + 1) * sizeof(C);
   {
     auto k = fft_strided<R, false, -1>;
@@ -525,7 +607,7 @@ static int poisson_run(Ctx* c, double* rhs, cudaStream_t st) {
   }
   // C: z forward + Poisson + z inverse; lines over kx, outer over ky
   {
-    const int lanes_z = std::max(1, std::min(32, FFT_ELEMS / nz));
+    const int lanes_z = strided_lanes<C>(nz);
     const size_t smem_z = (size_t)lanes_z * (nz + 1) * sizeof(C);
     auto k = fft_strided<R, true, -1>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_z);
@@ -1023,7 +1105,7 @@ int poisson_010(Ctx* c, double* rhs, cudaStream_t st) {
     k<<<nbx, FFT_THREADS, smem_x, st>>>(rhs, spec, nx, nlines, lpb, twx_f, twx_full);
   }
   // B: z forward; lines over kx, outer over y
-  const int lanes_z = std::max(1, std::min(32, FFT_ELEMS / nz));
+  const int lanes_z = strided_lanes<C>(nz);
   const size_t smem_z = (size_t)lanes_z * (nz + 1) * sizeof(C);
   const dim3 gz((nxh + lanes_z - 1) / lanes_z, nym);
   {

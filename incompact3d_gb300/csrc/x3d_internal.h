@@ -125,6 +125,7 @@ struct Ctx {
   float2* d_k2df[3] = {nullptr, nullptr, nullptr};  // k2 / transfer tables as hi/lo pairs
   float2* d_trdf[3] = {nullptr, nullptr, nullptr};
   int twid_n = 0;
+  void* d_inv[3] = {nullptr, nullptr, nullptr};  // poisson_000 factor tables: f64, f32, hi/lo f32
   void* fft_work = nullptr;  // complex spectrum buffer
   size_t fft_work_bytes = 0;
   Stretch st;
