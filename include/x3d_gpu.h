@@ -321,6 +321,17 @@ int x3d_solver_set_les(x3d_solver* s, int jles, double smagcst, double maxdsmagc
 /* Eddy viscosity and SGS force of the current velocity into device arrays of
  * N = nx*ny*nz doubles (for checks and output), stream-ordered. */
 int x3d_solver_les_fields(x3d_solver* s, double* nut, double* sgsx, double* sgsy, double* sgsz, void* stream);
+/* Restart state (restart, src/tools.f90:205-514): which = 0..2 velocity
+ * (ux, uy, uz), 3..5 the previous right-hand side (dux1(:,:,:,2), ... of
+ * AB2/AB3), 6..8 the one before (dux1(:,:,:,3), AB3 only), 9 the pressure
+ * pp3 on the pressure mesh (nxm*nym*nzm values).  on_device: 1 = device
+ * pointer, 0 = host.  X3D_ERR_STATE for a slot the time scheme does not keep. */
+int x3d_solver_get_field(x3d_solver* s, int which, double* out, int on_device);
+int x3d_solver_set_field(x3d_solver* s, int which, const double* in, int on_device);
+/* Completed time steps (itime - 1 of the reference's loop); set it when
+ * restarting so that AB3 does not repeat its Euler/AB2 start-up. */
+int x3d_solver_get_itime(x3d_solver* s);
+int x3d_solver_set_itime(x3d_solver* s, int itime);
 /* Bulk velocity measured by channel_cfr (before its correction) at each
  * sub-step of the last step; returns the number of values.  Synchronises. */
 int x3d_solver_bulk_velocity(x3d_solver* s, double* out, int capacity);

@@ -123,6 +123,10 @@ def load():
         lib.x3d_solver_bulk_velocity.argtypes = [P, P, I]
         lib.x3d_get_stretching.argtypes = [P, I, P, I]
         lib.x3d_solver_set_les.argtypes = [P, I, D, D]
+        lib.x3d_solver_get_field.argtypes = [P, I, P, I]
+        lib.x3d_solver_set_field.argtypes = [P, I, P, I]
+        lib.x3d_solver_get_itime.argtypes = [P]
+        lib.x3d_solver_set_itime.argtypes = [P, I]
         lib.x3d_solver_les_fields.argtypes = [P, P, P, P, P, P]
         _lib = lib
         return lib

@@ -1145,6 +1145,102 @@ int x3d_solver_get_velocity(x3d_solver* s, double* ux, double* uy, double* uz, i
   return X3D_OK;
 }
 
+// ---- restart state (src/tools.f90:205-514): history and pressure ---------
+__global__ void k_f32_to_f64(double* o, const float* a, long long n) {
+  GRID_STRIDE(i, n) o[i] = (double)a[i];
+}
+
+// which: 0..2 velocity, 3..5 previous right-hand side (dux-2, duy-2, duz-2),
+// 6..8 the one before (dux-3, ...), 9 pressure (nxm, nym, nzm).
+static int state_slot(SolverImpl* si, int which, void** ptr, long long* n, bool* f32) {
+  *f32 = false;
+  *n = si->N;
+  if (which >= 0 && which <= 2) {
+    *ptr = which == 0 ? si->ux : which == 1 ? si->uy : si->uz;
+    return X3D_OK;
+  }
+  if (which >= 3 && which <= 8) {
+    const int slot = which < 6 ? 1 : 2;
+    if (slot >= si->ntime) return X3D_ERR_STATE;
+    *ptr = si->H[(which - 3) % 3][slot];
+    *f32 = si->mixed();
+    return X3D_OK;
+  }
+  if (which == 9) {
+    *ptr = si->pp64;
+    *n = si->Np;
+    return X3D_OK;
+  }
+  return X3D_ERR_ARG;
+}
+
+int x3d_solver_get_field(x3d_solver* s, int which, double* out, int on_device) {
+  if (!s || !out) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  void* p = nullptr;
+  long long n = 0;
+  bool f32 = false;
+  int rc = state_slot(si, which, &p, &n, &f32);
+  if (rc != X3D_OK) return rc;
+  if (which <= 2) {
+    rc = stage64(si, nullptr);
+    if (rc != X3D_OK) return rc;
+  }
+  const double* src = (const double*)p;
+  if (f32) {
+    // binary32 history of the mixed solver, widened through a temporary
+    double* stage = nullptr;
+    if (cudaMalloc(&stage, (size_t)n * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
+    k_f32_to_f64<<<pw_blocks(si->c, n), 256>>>(stage, (const float*)p, n);
+    rc = cuda_status(cudaMemcpy(out, stage, (size_t)n * sizeof(double),
+                                on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
+    cudaFree(stage);
+    return rc;
+  }
+  return cuda_status(cudaMemcpy(out, src, (size_t)n * sizeof(double),
+                                on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
+}
+
+int x3d_solver_set_field(x3d_solver* s, int which, const double* in, int on_device) {
+  if (!s || !in) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  void* p = nullptr;
+  long long n = 0;
+  bool f32 = false;
+  int rc = state_slot(si, which, &p, &n, &f32);
+  if (rc != X3D_OK) return rc;
+  const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (f32) {
+    double* stage = nullptr;
+    if (cudaMalloc(&stage, (size_t)n * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
+    rc = cuda_status(cudaMemcpy(stage, in, (size_t)n * sizeof(double), k));
+    if (rc == X3D_OK) {
+      k_to32<<<pw_blocks(si->c, n), 256>>>((float*)p, stage, n);
+      rc = cuda_status(cudaDeviceSynchronize());
+    }
+    cudaFree(stage);
+    return rc;
+  }
+  if (which <= 2 && si->mixed()) {
+    rc = stage64(si, nullptr);  // the other components' staging must be current
+    if (rc != X3D_OK) return rc;
+  }
+  rc = cuda_status(cudaMemcpy(p, in, (size_t)n * sizeof(double), k));
+  if (rc == X3D_OK && which <= 2 && si->mixed()) rc = sync_copies(si);
+  return rc;
+}
+
+int x3d_solver_get_itime(x3d_solver* s) {
+  if (!s) return X3D_ERR_ARG;
+  return s->impl.itime;
+}
+
+int x3d_solver_set_itime(x3d_solver* s, int itime) {
+  if (!s || itime < 0) return X3D_ERR_ARG;
+  s->impl.itime = itime;
+  return X3D_OK;
+}
+
 int x3d_solver_init_tgv(x3d_solver* s) {
   if (!s) return X3D_ERR_ARG;
   SolverImpl* si = &s->impl;

@@ -64,6 +64,8 @@ class Context:
         check(self.lib.x3d_ctx_create(ctypes.byref(g), ctypes.byref(o), ctypes.byref(h)), "x3d_ctx_create")
         self.h = h
         self.n = (nx, ny, nz)
+        self.L = (xlx, yly, zlz)
+        self.istret, self.beta = istret, beta
         self.bc = bc
         self.nm = tuple(n if b == (0, 0) else n - 1 for n, b in zip(self.n, bc))
 
@@ -227,6 +229,7 @@ class Solver:
     def __init__(self, ctx, dt, xnu, itimescheme=3, precision=PREC_FP64):
         self.ctx = ctx
         self.lib = ctx.lib
+        self.itimescheme, self.dt, self.xnu = itimescheme, dt, xnu
         o = _lib.SolverOpts(itimescheme, dt, xnu, precision)
         h = ctypes.c_void_p()
         check(self.lib.x3d_solver_create(ctx.h, ctypes.byref(o), ctypes.byref(h)), "x3d_solver_create")
@@ -276,6 +279,28 @@ class Solver:
         """Channel case: constant flow rate control and the spin-up rotation."""
         check(self.lib.x3d_solver_set_channel(self.h, target_ub, wrotation, spinup_time),
               "x3d_solver_set_channel")
+
+    def get_field(self, which):
+        """Restart state slot as a host array: 0..2 velocity, 3..5 / 6..8 the
+        AB history, 9 the pressure (pressure mesh)."""
+        nx, ny, nz = self.ctx.n
+        shp = (nz, ny, nx) if which != 9 else tuple(reversed(self.ctx.nm))
+        out = np.empty(shp)
+        check(self.lib.x3d_solver_get_field(self.h, which, out.ctypes.data_as(ctypes.c_void_p), 0),
+              "x3d_solver_get_field")
+        return out
+
+    def set_field(self, which, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        check(self.lib.x3d_solver_set_field(self.h, which, a.ctypes.data_as(ctypes.c_void_p), 0),
+              "x3d_solver_set_field")
+
+    def set_itime(self, itime):
+        check(self.lib.x3d_solver_set_itime(self.h, int(itime)), "x3d_solver_set_itime")
+
+    @property
+    def itime(self):
+        return check(self.lib.x3d_solver_get_itime(self.h), "x3d_solver_get_itime")
 
     def set_les(self, jles, smagcst=0.14, maxdsmagcst=0.3):
         """Explicit LES model: 1 Smagorinsky, 3 dynamic Smagorinsky, 0 off."""
