@@ -13,6 +13,9 @@
 //     instead of loading six coefficient vectors per row;
 //   * the Sherman-Morrison correction is applied only to chunks where the
 //     precomputed vector is non-zero in this precision.
+// The chunk solve is a device function (fast_solve) so that one kernel can
+// run several operators on the same lines (rhs_fast, the momentum right-hand
+// side: three solves per line, one HBM pass per input field).
 #pragma once
 #include "x3d_line_kernel.cuh"
 
@@ -21,12 +24,9 @@ namespace lk {
 
 constexpr int FCHUNKS = 16;
 
+// Coefficients of one operator for the fast path.
 template <typename T>
-struct FastArgs {
-  const T* in;
-  T* out;
-  long long sa, sb, rs;  // line (a, b) offset and row stride (same for in and out)
-  int n, na;
+struct FastOp {
   const T *s, *f, *w, *pf, *qb, *rsm;  // per-row vectors (non-uniform chunks)
   T ca, cb, cc, cd, alpha, den;
   T s_inf, f_inf, w_inf, g_inf;  // interior factors; g = -(f*w)
@@ -34,7 +34,16 @@ struct FastArgs {
   T qbs[FCHUNKS];                // qb at each chunk's first row
   int mode[FCHUNKS];             // bit0: uniform factors, bit1: SM vector non-zero
   int nterms_int;
-  Fuse<T> fz;                    // optional product on load / combination on store
+};
+
+template <typename T>
+struct FastArgs {
+  const T* in;
+  T* out;
+  long long sa, sb, rs;  // line (a, b) offset and row stride (same for in and out)
+  int n, na;
+  FastOp<T> op;
+  Fuse<T> fz;  // optional product on load / combination on store
 };
 
 template <int KIND>
@@ -44,7 +53,7 @@ struct Halo {
 
 // Interior stencil on the register window: w[j] holds u[r0 - lo + j].
 template <typename T, int KIND, int LO>
-__device__ __forceinline__ T interior_w(const T* w, int k, const FastArgs<T>& p) {
+__device__ __forceinline__ T interior_w(const T* w, int k, const FastOp<T>& p) {
 #define W_(d) w[k + LO + (d)]
   if constexpr (KIND == K_DER1) {
     return p.ca * (W_(1) - W_(-1)) + p.cb * (W_(2) - W_(-2));
@@ -71,77 +80,26 @@ __device__ __forceinline__ T interior_w(const T* w, int k, const FastArgs<T>& p)
 #undef W_
 }
 
-template <typename T, int KIND, bool XL, int L>
-__global__ void __launch_bounds__(LANES* FCHUNKS, 2) line_fast(const __grid_constant__ FastArgs<T> p) {
-  constexpr int LO = Halo<KIND>::lo, HI = Halo<KIND>::hi;
-  constexpr int WN = L + LO + HI;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* cfw = reinterpret_cast<T*>(smem_raw);
-  T* cbw = cfw + FCHUNKS * LANES;
-  T* ends = cbw + FCHUNKS * LANES;
-  T* tile = ends + 2 * LANES;  // x lines only: [n][LD]
+// Row index of window slot j of chunk ch (periodic wrap only in the first and
+// last chunk, whose halos cross the line ends).
+__device__ __forceinline__ int wrow(int r, int n, bool edge) {
+  return edge ? ((r < 0) ? r + n : (r >= n ? r - n : r)) : r;
+}
 
-  const int lane = threadIdx.x, ch = threadIdx.y;
-  const int n = p.n;
-  const int a0 = blockIdx.x * LANES;
-  const long long b = blockIdx.y;
-  const int nl = min(LANES, p.na - a0);
+// Solve of this thread's chunk (rows ch*L .. ch*L+L-1) of one line:
+// v = A^{-1} (B u) with u in the register window w (w[j] = u[r0 - LO + j]).
+// Uses the block's carry arrays and three block barriers; every thread of
+// the block must call it.
+template <typename T, int KIND, int L>
+__device__ __forceinline__ void fast_solve(const T* w, T* v, const FastOp<T>& p, T* cfw, T* cbw, T* ends, int ch,
+                                           int lane) {
+  constexpr int LO = Halo<KIND>::lo;
   const int r0 = ch * L;
   const int mode = p.mode[ch];
-
-  // 1. register window u[r0-LO .. r0+L+HI) (periodic wrap)
-  T w[WN];
-  if (!XL) {
-    const bool ok = lane < nl;
-    const long long off = (ok ? (long long)(a0 + lane) * p.sa : 0) + b * p.sb;
-    const T* src = p.in + off;
-    if (p.fz.in2) {
-      const T* src2 = p.fz.in2 + off;
-#pragma unroll
-      for (int j = 0; j < WN; ++j) {
-        int r = r0 - LO + j;
-        r = (r < 0) ? r + n : (r >= n ? r - n : r);
-        w[j] = ok ? src[(long long)r * p.rs] * src2[(long long)r * p.rs] : T(0);
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < WN; ++j) {
-        int r = r0 - LO + j;
-        r = (r < 0) ? r + n : (r >= n ? r - n : r);
-        w[j] = ok ? src[(long long)r * p.rs] : T(0);
-      }
-    }
-  } else {
-    const long long off = (long long)a0 * p.sa + b * p.sb;
-    const T* src = p.in + off;
-    const T* src2 = p.fz.in2 ? p.fz.in2 + off : nullptr;
-    for (int l = ch; l < LANES; l += FCHUNKS) {
-      if (l < nl) {
-        if (src2) {
-          for (int r = lane; r < n; r += LANES)
-            tile[r * LD + l] = src[(long long)l * p.sa + r] * src2[(long long)l * p.sa + r];
-        } else {
-          for (int r = lane; r < n; r += LANES) tile[r * LD + l] = src[(long long)l * p.sa + r];
-        }
-      } else {
-        for (int r = lane; r < n; r += LANES) tile[r * LD + l] = T(0);
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < WN; ++j) {
-      int r = r0 - LO + j;
-      r = (r < 0) ? r + n : (r >= n ? r - n : r);
-      w[j] = tile[r * LD + lane];
-    }
-  }
-
-  // 2. right-hand side
-  T v[L];
+  // right-hand side
 #pragma unroll
   for (int k = 0; k < L; ++k) v[k] = interior_w<T, KIND, LO>(w, k, p);
-
-  // 3. forward elimination + carry scan + fix-up
+  // forward elimination + carry scan + fix-up
   T y = T(0);
   if (mode & 1) {
 #pragma unroll
@@ -165,8 +123,7 @@ __global__ void __launch_bounds__(LANES* FCHUNKS, 2) line_fast(const __grid_cons
       for (int k = 0; k < L; ++k) v[k] = v[k] + p.pf[r0 + k] * cin;
     }
   }
-
-  // 4. back substitution + carry scan + fix-up
+  // back substitution + carry scan + fix-up
   T x = T(0);
   if (mode & 1) {
 #pragma unroll
@@ -189,8 +146,7 @@ __global__ void __launch_bounds__(LANES* FCHUNKS, 2) line_fast(const __grid_cons
       for (int k = 0; k < L; ++k) v[k] = v[k] + p.qb[r0 + k] * cin;
     }
   }
-
-  // 5. Sherman-Morrison
+  // Sherman-Morrison
   if (ch == 0) ends[lane] = v[0];
   if (ch == FCHUNKS - 1) ends[LANES + lane] = v[L - 1];
   __syncthreads();
@@ -199,6 +155,70 @@ __global__ void __launch_bounds__(LANES* FCHUNKS, 2) line_fast(const __grid_cons
 #pragma unroll
     for (int k = 0; k < L; ++k) v[k] = v[k] - sx * p.rsm[r0 + k];
   }
+}
+
+template <typename T, int KIND, bool XL, int L>
+__global__ void __launch_bounds__(LANES* FCHUNKS, 2) line_fast(const __grid_constant__ FastArgs<T> p) {
+  constexpr int LO = Halo<KIND>::lo, HI = Halo<KIND>::hi;
+  constexpr int WN = L + LO + HI;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* cfw = reinterpret_cast<T*>(smem_raw);
+  T* cbw = cfw + FCHUNKS * LANES;
+  T* ends = cbw + FCHUNKS * LANES;
+  T* tile = ends + 2 * LANES;  // x lines only: [n][LD]
+
+  const int lane = threadIdx.x, ch = threadIdx.y;
+  const int n = p.n;
+  const int a0 = blockIdx.x * LANES;
+  const long long b = blockIdx.y;
+  const int nl = min(LANES, p.na - a0);
+  const int r0 = ch * L;
+  const bool edge = (ch == 0 || ch == FCHUNKS - 1);
+
+  // 1. register window u[r0-LO .. r0+L+HI) (periodic wrap)
+  T w[WN];
+  if (!XL) {
+    const bool ok = lane < nl;
+    const long long off = (ok ? (long long)(a0 + lane) * p.sa : 0) + b * p.sb;
+    const T* src = p.in + off;
+    if (p.fz.in2) {
+      const T* src2 = p.fz.in2 + off;
+#pragma unroll
+      for (int j = 0; j < WN; ++j) {
+        const int r = wrow(r0 - LO + j, n, edge);
+        w[j] = ok ? src[(long long)r * p.rs] * src2[(long long)r * p.rs] : T(0);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < WN; ++j) {
+        const int r = wrow(r0 - LO + j, n, edge);
+        w[j] = ok ? src[(long long)r * p.rs] : T(0);
+      }
+    }
+  } else {
+    const long long off = (long long)a0 * p.sa + b * p.sb;
+    const T* src = p.in + off;
+    const T* src2 = p.fz.in2 ? p.fz.in2 + off : nullptr;
+    for (int l = ch; l < LANES; l += FCHUNKS) {
+      if (l < nl) {
+        if (src2) {
+          for (int r = lane; r < n; r += LANES)
+            tile[r * LD + l] = src[(long long)l * p.sa + r] * src2[(long long)l * p.sa + r];
+        } else {
+          for (int r = lane; r < n; r += LANES) tile[r * LD + l] = src[(long long)l * p.sa + r];
+        }
+      } else {
+        for (int r = lane; r < n; r += LANES) tile[r * LD + l] = T(0);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < WN; ++j) w[j] = tile[wrow(r0 - LO + j, n, edge) * LD + lane];
+  }
+
+  // 2-5. solve
+  T v[L];
+  fast_solve<T, KIND, L>(w, v, p.op, cfw, cbw, ends, ch, lane);
 
   // 6. store (with the optional combination epilogue)
   if (!XL) {
@@ -206,7 +226,7 @@ __global__ void __launch_bounds__(LANES* FCHUNKS, 2) line_fast(const __grid_cons
       const long long off = (long long)(a0 + lane) * p.sa + b * p.sb;
       T* dst = p.out + off;
       if (p.fz.active) {
-        // operands are read in groups of 8 rows before any store of the group:
+        // operands are read in groups of 4 rows before any store of the group:
         // the output may alias a1/a2, so the compiler cannot batch them itself
         constexpr int G = 4;
 #pragma unroll
@@ -283,6 +303,12 @@ int fast_dispatch_xl(const FastArgs<T>& a, bool xl, int L, dim3 grid, size_t sme
   if (L == 16) return launch_fast_k<T, KIND, false, 16>(a, grid, smem, st);
   return launch_fast_k<T, KIND, false, 32>(a, grid, smem, st);
 }
+
+// Fast-path coefficients of a periodic FP32 plan, and the line geometry of an
+// axis (x3d_lines.cu).
+void fill_fast_op(const OpPlan* p, FastOp<float>& a);
+void fast_geometry(int axis, int n, const int* dims_in, long long* sa, long long* sb, long long* rs, int* na,
+                   dim3* grid);
 
 // Instantiated per operator kind in x3d_lines_<kind>.cu (FP32 only).
 template <int KIND>

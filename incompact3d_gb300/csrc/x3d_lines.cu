@@ -9,6 +9,55 @@ namespace x3d {
 
 using namespace lk;
 
+namespace lk {
+// Fast-path coefficients of a (periodic, FP32) plan.
+void fill_fast_op(const OpPlan* p, FastOp<float>& a) {
+  const int n = p->nout;
+  const int L = n / FCHUNKS;
+  const float* dv = p->dev32;
+  a.s = dv; a.f = dv + n; a.w = dv + 2 * n; a.pf = dv + 3 * n; a.qb = dv + 4 * n; a.rsm = dv + 5 * n;
+  a.ca = (float)p->ca; a.cb = (float)p->cb; a.cc = (float)p->cc; a.cd = (float)p->cd;
+  a.alpha = (float)p->alpha;
+  a.den = (float)p->den;
+  a.nterms_int = 4;
+  if (p->kind == K_DER2 && p->cc == 0.0 && p->cd == 0.0) a.nterms_int = 2;
+  if ((p->kind == K_IVP || p->kind == K_IPV) && p->cd == 0.0) a.nterms_int = 3;
+  const int mid = n / 2;
+  a.s_inf = (float)p->s[mid];
+  a.f_inf = (float)p->f[mid];
+  a.w_inf = (float)p->w[mid];
+  a.g_inf = (float)(-(p->f[mid] * p->w[mid]));
+  for (int c = 0; c < FCHUNKS; ++c) {
+    const int s0 = c * L, e0 = s0 + L - 1;
+    a.pfe[c] = (float)p->pf[e0];
+    a.qbs[c] = (float)p->qb[s0];
+    bool uni = true, sm = false;
+    for (int r = s0; r <= e0; ++r) {
+      uni = uni && (float)p->s[r] == a.s_inf && (float)p->f[r] == a.f_inf && (float)p->w[r] == a.w_inf;
+      sm = sm || (float)p->rsm[r] != 0.0f;
+    }
+    a.mode[c] = (uni ? 1 : 0) | (sm ? 2 : 0);
+  }
+}
+
+// Line geometry of an axis for the fast kernels: lines (a, b), row stride.
+void fast_geometry(int axis, int n, const int* dims_in, long long* sa, long long* sb, long long* rs, int* na,
+                   dim3* grid) {
+  const long long nx = dims_in[0], ny = dims_in[1], nz = dims_in[2];
+  if (axis == 0) {
+    *na = (int)ny; *sa = n; *sb = ny * n; *rs = 1;
+    *grid = dim3((unsigned)((ny + LANES - 1) / LANES), (unsigned)nz);
+  } else if (axis == 1) {
+    *na = (int)nx; *sa = 1; *sb = nx * n; *rs = nx;
+    *grid = dim3((unsigned)((nx + LANES - 1) / LANES), (unsigned)nz);
+  } else {
+    *na = (int)nx; *sa = 1; *sb = nx; *rs = nx * ny;
+    *grid = dim3((unsigned)((nx + LANES - 1) / LANES), (unsigned)ny);
+  }
+}
+
+}  // namespace lk
+
 namespace {
 
 template <typename T>
@@ -48,44 +97,11 @@ int launch_fast(OpPlan* p, float* out, const float* in, const int* dims_in, cuda
   a.in = in;
   a.out = out;
   a.n = n;
-  const long long nx = dims_in[0], ny = dims_in[1], nz = dims_in[2];
   dim3 grid;
   const bool xl = (p->axis == 0);
-  if (p->axis == 0) {
-    a.na = (int)ny; a.sa = n; a.sb = ny * n; a.rs = 1;
-    grid = dim3((unsigned)((ny + LANES - 1) / LANES), (unsigned)nz);
-  } else if (p->axis == 1) {
-    a.na = (int)nx; a.sa = 1; a.sb = nx * n; a.rs = nx;
-    grid = dim3((unsigned)((nx + LANES - 1) / LANES), (unsigned)nz);
-  } else {
-    a.na = (int)nx; a.sa = 1; a.sb = nx; a.rs = nx * ny;
-    grid = dim3((unsigned)((nx + LANES - 1) / LANES), (unsigned)ny);
-  }
+  fast_geometry(p->axis, n, dims_in, &a.sa, &a.sb, &a.rs, &a.na, &grid);
   if (grid.y > 65535) return X3D_ERR_UNSUPPORTED;
-  const float* dv = p->dev32;
-  a.s = dv; a.f = dv + n; a.w = dv + 2 * n; a.pf = dv + 3 * n; a.qb = dv + 4 * n; a.rsm = dv + 5 * n;
-  a.ca = (float)p->ca; a.cb = (float)p->cb; a.cc = (float)p->cc; a.cd = (float)p->cd;
-  a.alpha = (float)p->alpha;
-  a.den = (float)p->den;
-  a.nterms_int = 4;
-  if (p->kind == K_DER2 && p->cc == 0.0 && p->cd == 0.0) a.nterms_int = 2;
-  if ((p->kind == K_IVP || p->kind == K_IPV) && p->cd == 0.0) a.nterms_int = 3;
-  const int mid = n / 2;
-  a.s_inf = (float)p->s[mid];
-  a.f_inf = (float)p->f[mid];
-  a.w_inf = (float)p->w[mid];
-  a.g_inf = (float)(-(p->f[mid] * p->w[mid]));
-  for (int c = 0; c < FCHUNKS; ++c) {
-    const int s0 = c * L, e0 = s0 + L - 1;
-    a.pfe[c] = (float)p->pf[e0];
-    a.qbs[c] = (float)p->qb[s0];
-    bool uni = true, sm = false;
-    for (int r = s0; r <= e0; ++r) {
-      uni = uni && (float)p->s[r] == a.s_inf && (float)p->f[r] == a.f_inf && (float)p->w[r] == a.w_inf;
-      sm = sm || (float)p->rsm[r] != 0.0f;
-    }
-    a.mode[c] = (uni ? 1 : 0) | (sm ? 2 : 0);
-  }
+  fill_fast_op(p, a.op);
   if (fz) a.fz = *fz;
   const size_t smem = fast_smem<float>(n, xl);
   return fdispatch(a, p->kind, xl, L, grid, smem, st);
@@ -125,7 +141,7 @@ int finalize_plan(OpPlan* p) {
 }
 
 // Device copies of a plan's vectors, made on first launch.
-static int upload_plan(OpPlan* p) {
+int upload_plan(OpPlan* p) {
   if (p->dev64) return X3D_OK;
   const int n = p->nout;
   std::vector<double> h64(6 * (size_t)n);

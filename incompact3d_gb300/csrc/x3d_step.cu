@@ -537,6 +537,40 @@ static int momentum_rhs(SolverImpl* s, const T* const* u, T* const* H, cudaStrea
   const T one = T(1), mhalf = T(-0.5), zero = T(0);
   // stretched mesh: dery multiplies by ppy; d2/dy2 gets the pp2y / pp4y terms
   const T* ppy = ymetric<T>(s, 0);
+  if (std::is_same<T, float>::value && !ppy) {
+    // FP32 periodic lines: one fused kernel per axis runs the three solves of
+    // a line (Z, then Y, then X into the history slot)
+    bool fused = true;
+    for (int q = 0; q < 3 && fused; ++q) {
+      const int pu[3] = {q == 0 ? 0 : 1, q == 1 ? 0 : 1, q == 2 ? 0 : 1};
+      OpPlan* P[3][3];
+      for (int ax = 0; ax < 3; ++ax) {
+        RC(get_plan(c, ax, K_DER1, 1 - pu[ax], default_coefset(K_DER1, 1 - pu[ax]), &P[ax][0]));
+        RC(get_plan(c, ax, K_DER1, pu[ax], default_coefset(K_DER1, pu[ax]), &P[ax][1]));
+        RC(get_plan(c, ax, K_DER2, pu[ax], default_coefset(K_DER2, pu[ax]), &P[ax][2]));
+      }
+      float* tzf = (float*)tz;
+      const float* uf[3] = {(const float*)u[0], (const float*)u[1], (const float*)u[2]};
+      const float* uqf = uf[q];
+      int rc = rhs_axis_fast(c, P[2][0], P[2][1], P[2][2], tzf, uf[2], uqf, nullptr, (float)xnu, dims, st);
+      if (rc == X3D_ERR_UNSUPPORTED && q == 0) {
+        fused = false;
+        break;
+      }
+      RC(rc);
+      RC(rhs_axis_fast(c, P[1][0], P[1][1], P[1][2], tzf, uf[1], uqf, tzf, (float)xnu, dims, st));
+      s->launches += 2;
+      // x lines: the fused form needs two transposed tiles (one CTA per SM),
+      // which measured slower than the three single-solve kernels
+      Fuse<T> f = fz_prod<T>(u[q]);
+      RC(op<T>(s, 0, K_DER1, 1 - pu[0], t1, u[0], dims, st, &f));
+      f = fz_comb<T>(zero, t1, one, nullptr, zero, u[0]);
+      RC(op<T>(s, 0, K_DER1, pu[0], tg, u[q], dims, st, &f));
+      f = fz_comb<T>(xnu, tz, one, tg, mhalf, nullptr);
+      RC(op<T>(s, 0, K_DER2, pu[0], H[q], u[q], dims, st, &f));
+    }
+    if (fused) return cuda_status(cudaGetLastError());
+  }
   for (int q = 0; q < 3; ++q) {
     const T* uq = u[q];
     const int pu[3] = {q == 0 ? 0 : 1, q == 1 ? 0 : 1, q == 2 ? 0 : 1};  // parity of d_j u_q
