@@ -34,6 +34,8 @@ struct FastOp {
   T qbs[FCHUNKS];                // qb at each chunk's first row
   int mode[FCHUNKS];             // bit0: uniform factors, bit1: SM vector non-zero
   int nterms_int;
+  T pw[32];                      // uniform chunks: forward fix-up (-s)^(k+1)
+  T qw[32];                      // uniform chunks: backward fix-up g^(L-k)
 };
 
 template <typename T>
@@ -86,6 +88,26 @@ __device__ __forceinline__ int wrow(int r, int n, bool edge) {
   return edge ? ((r < 0) ? r + n : (r >= n ? r - n : r)) : r;
 }
 
+// Register window of a y/z line from global memory: w[j] = u[r0m + j]
+// (times u2 when given), rows wrapped only in the edge chunks.  Lanes past
+// the last line read a
+// valid line instead (their results are never stored, and the chunk carries
+// are per lane).
+template <typename T, int WN>
+__device__ __forceinline__ void load_window(T* w, const T* src, const T* src2, int r0m, int n, long long rs,
+                                            bool edge) {
+  if (src2) {
+#pragma unroll
+    for (int j = 0; j < WN; ++j) {
+      const long long o = (long long)wrow(r0m + j, n, edge) * rs;
+      w[j] = src[o] * src2[o];
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < WN; ++j) w[j] = src[(long long)wrow(r0m + j, n, edge) * rs];
+  }
+}
+
 // Solve of this thread's chunk (rows ch*L .. ch*L+L-1) of one line:
 // v = A^{-1} (B u) with u in the register window w (w[j] = u[r0 - LO + j]).
 // Uses the block's carry arrays and three block barriers; every thread of
@@ -114,10 +136,8 @@ __device__ __forceinline__ void fast_solve(const T* w, T* v, const FastOp<T>& p,
     T cin = T(0);
     for (int c = 0; c < ch; ++c) cin = cfw[c * LANES + lane] + p.pfe[c] * cin;
     if (mode & 1) {
-      const T m = -p.s_inf;
-      T P = m;
 #pragma unroll
-      for (int k = 0; k < L; ++k) { v[k] = v[k] + P * cin; P = P * m; }
+      for (int k = 0; k < L; ++k) v[k] = v[k] + p.pw[k] * cin;
     } else {
 #pragma unroll
       for (int k = 0; k < L; ++k) v[k] = v[k] + p.pf[r0 + k] * cin;
@@ -138,9 +158,8 @@ __device__ __forceinline__ void fast_solve(const T* w, T* v, const FastOp<T>& p,
     T cin = T(0);
     for (int c = FCHUNKS - 1; c > ch; --c) cin = cbw[c * LANES + lane] + p.qbs[c] * cin;
     if (mode & 1) {
-      T Q = p.g_inf;
 #pragma unroll
-      for (int k = L - 1; k >= 0; --k) { v[k] = v[k] + Q * cin; Q = Q * p.g_inf; }
+      for (int k = 0; k < L; ++k) v[k] = v[k] + p.qw[k] * cin;
     } else {
 #pragma unroll
       for (int k = 0; k < L; ++k) v[k] = v[k] + p.qb[r0 + k] * cin;
@@ -180,21 +199,7 @@ __global__ void __launch_bounds__(LANES* FCHUNKS, 2) line_fast(const __grid_cons
   if (!XL) {
     const bool ok = lane < nl;
     const long long off = (ok ? (long long)(a0 + lane) * p.sa : 0) + b * p.sb;
-    const T* src = p.in + off;
-    if (p.fz.in2) {
-      const T* src2 = p.fz.in2 + off;
-#pragma unroll
-      for (int j = 0; j < WN; ++j) {
-        const int r = wrow(r0 - LO + j, n, edge);
-        w[j] = ok ? src[(long long)r * p.rs] * src2[(long long)r * p.rs] : T(0);
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < WN; ++j) {
-        const int r = wrow(r0 - LO + j, n, edge);
-        w[j] = ok ? src[(long long)r * p.rs] : T(0);
-      }
-    }
+    load_window<T, WN>(w, p.in + off, p.fz.in2 ? p.fz.in2 + off : nullptr, r0 - LO, n, p.rs, edge);
   } else {
     const long long off = (long long)a0 * p.sa + b * p.sb;
     const T* src = p.in + off;

@@ -38,6 +38,19 @@ void fill_fast_op(const OpPlan* p, FastOp<float>& a) {
     }
     a.mode[c] = (uni ? 1 : 0) | (sm ? 2 : 0);
   }
+  // fix-up factors of uniform chunks, by the same running products in binary32
+  const float m = -a.s_inf;
+  float P = m;
+  for (int k = 0; k < 32; ++k) {
+    a.pw[k] = (k < L) ? P : 0.f;
+    P = P * m;
+  }
+  float Q = a.g_inf;
+  for (int k = L - 1; k >= 0; --k) {
+    a.qw[k] = Q;
+    Q = Q * a.g_inf;
+  }
+  for (int k = L; k < 32; ++k) a.qw[k] = 0.f;
 }
 
 // Line geometry of an axis for the fast kernels: lines (a, b), row stride.

@@ -55,36 +55,28 @@ __global__ void __launch_bounds__(LANES* FCHUNKS, 2) rhs_fast(const __grid_const
     const float* ua = p.ua + off;
     {
       float w[W1];
-#pragma unroll
-      for (int j = 0; j < W1; ++j) {
-        const long long r = wrow(r0 - 2 + j, n, edge);
-        w[j] = ok ? q[r * p.rs] * ua[r * p.rs] : 0.f;
-      }
+      load_window<float, W1>(w, q, ua, r0 - 2, n, p.rs, edge);
       fast_solve<float, K_DER1, L>(w, v, p.A, cfw, cbw, ends, ch, lane);
     }
 #pragma unroll
     for (int k = 0; k < L; ++k) stash[k * NT + tid] = v[k];
     {
       float w[W1];
-#pragma unroll
-      for (int j = 0; j < W1; ++j) {
-        const long long r = wrow(r0 - 2 + j, n, edge);
-        w[j] = ok ? q[r * p.rs] : 0.f;
-      }
+      load_window<float, W1>(w, q, nullptr, r0 - 2, n, p.rs, edge);
       fast_solve<float, K_DER1, L>(w, v, p.B, cfw, cbw, ends, ch, lane);
     }
+    {
+      const float* ub = ua + (long long)r0 * p.rs;
+      const int s32 = (int)p.rs;
 #pragma unroll
-    for (int k = 0; k < L; ++k) {
-      const float uj = ok ? ua[(long long)(r0 + k) * p.rs] : 0.f;
-      stash[k * NT + tid] = stash[k * NT + tid] + uj * v[k];
+      for (int k = 0; k < L; ++k) {
+        const float uj = ub[k * s32];
+        stash[k * NT + tid] = stash[k * NT + tid] + uj * v[k];
+      }
     }
     {
       float w[W2];
-#pragma unroll
-      for (int j = 0; j < W2; ++j) {
-        const long long r = wrow(r0 - 4 + j, n, edge);
-        w[j] = ok ? q[r * p.rs] : 0.f;
-      }
+      load_window<float, W2>(w, q, nullptr, r0 - 4, n, p.rs, edge);
       fast_solve<float, K_DER2, L>(w, v, p.C, cfw, cbw, ends, ch, lane);
     }
     if (ok) {
@@ -167,6 +159,217 @@ __global__ void __launch_bounds__(LANES* FCHUNKS, 2) rhs_fast(const __grid_const
   }
 }
 
+// ---- x lines: one warp per line -------------------------------------------
+// For x lines the line is contiguous in memory, so a warp can own one line:
+// the line is read (and the result written) coalesced through a padded
+// per-warp buffer, lane t holds rows t*L .. t*L+L-1 (n = 32 L) in registers,
+// and the chunk carries are combined with a warp-shuffle scan of the affine
+// maps c_out = pf_end * c_in + y_end (Kogge-Stone, 5 steps): no block barrier.
+constexpr int XCH = 32;  // chunks per line = lanes
+
+struct WarpOp {
+  const float *s, *f, *w, *pf, *qb, *rsm;
+  float ca, cb, cc, cd, alpha, den;
+  float s_inf, f_inf, w_inf, g_inf;
+  float pfe[XCH], qbs[XCH];
+  int mode[XCH];
+  int nterms_int;
+};
+
+struct RhsXArgs {
+  const float *ua, *uq, *a1;
+  float* out;
+  long long sa, sb;  // line and plane strides (row stride 1)
+  int n, na;
+  WarpOp A, B, C;
+  float nu;
+};
+
+// Inclusive scan of affine maps x -> a x + b over the lanes (lane order
+// forward when DOWN is false, backward when true); returns the carry into
+// this lane (exclusive result).
+template <bool DOWN>
+__device__ __forceinline__ float carry_scan(float a, float b, int lane) {
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const float pa = DOWN ? __shfl_down_sync(0xffffffffu, a, d) : __shfl_up_sync(0xffffffffu, a, d);
+    const float pb = DOWN ? __shfl_down_sync(0xffffffffu, b, d) : __shfl_up_sync(0xffffffffu, b, d);
+    const bool in = DOWN ? (lane + d < 32) : (lane >= d);
+    if (in) {
+      b = a * pb + b;
+      a = a * pa;
+    }
+  }
+  const float e = DOWN ? __shfl_down_sync(0xffffffffu, b, 1) : __shfl_up_sync(0xffffffffu, b, 1);
+  return (DOWN ? lane == 31 : lane == 0) ? 0.f : e;
+}
+
+template <int KIND, int LO>
+__device__ __forceinline__ float interior_x(const float* w, int k, const WarpOp& p) {
+#define W_(d) w[k + LO + (d)]
+  if constexpr (KIND == K_DER1) {
+    return p.ca * (W_(1) - W_(-1)) + p.cb * (W_(2) - W_(-2));
+  } else {
+    const float ur = W_(0);
+    float acc = p.ca * (W_(1) - ur - ur + W_(-1)) + p.cb * (W_(2) - ur - ur + W_(-2));
+    if (p.nterms_int > 2) acc = acc + p.cc * (W_(3) - ur - ur + W_(-3)) + p.cd * (W_(4) - ur - ur + W_(-4));
+    return acc;
+  }
+#undef W_
+}
+
+// Solve of lane t's chunk of the warp's line; w[j] = u[t*L - LO + j].
+template <int KIND, int L>
+__device__ __forceinline__ void warp_solve(const float* w, float* v, const WarpOp& p, int lane) {
+  constexpr int LO = Halo<KIND>::lo;
+  const int r0 = lane * L;
+  const int mode = p.mode[lane];
+#pragma unroll
+  for (int k = 0; k < L; ++k) v[k] = interior_x<KIND, LO>(w, k, p);
+  float y = 0.f;
+  if (mode & 1) {
+#pragma unroll
+    for (int k = 0; k < L; ++k) { y = v[k] - p.s_inf * y; v[k] = y; }
+  } else {
+#pragma unroll
+    for (int k = 0; k < L; ++k) { y = v[k] - p.s[r0 + k] * y; v[k] = y; }
+  }
+  float cin = carry_scan<false>(p.pfe[lane], y, lane);
+  // fix-up factors of this chunking (L rows) as running products
+  if (mode & 1) {
+    const float m = -p.s_inf;
+    float P = m;
+#pragma unroll
+    for (int k = 0; k < L; ++k) { v[k] = v[k] + P * cin; P = P * m; }
+  } else {
+    float P = 1.f;
+#pragma unroll
+    for (int k = 0; k < L; ++k) { P = P * (-p.s[r0 + k]); v[k] = v[k] + P * cin; }
+  }
+  float x = 0.f;
+  if (mode & 1) {
+#pragma unroll
+    for (int k = L - 1; k >= 0; --k) { x = (v[k] - p.f_inf * x) * p.w_inf; v[k] = x; }
+  } else {
+#pragma unroll
+    for (int k = L - 1; k >= 0; --k) { x = (v[k] - p.f[r0 + k] * x) * p.w[r0 + k]; v[k] = x; }
+  }
+  cin = carry_scan<true>(p.qbs[lane], x, lane);
+  if (mode & 1) {
+    float Q = p.g_inf;
+#pragma unroll
+    for (int k = L - 1; k >= 0; --k) { v[k] = v[k] + Q * cin; Q = Q * p.g_inf; }
+  } else {
+    float Q = 1.f;
+#pragma unroll
+    for (int k = L - 1; k >= 0; --k) { Q = Q * (-(p.f[r0 + k] * p.w[r0 + k])); v[k] = v[k] + Q * cin; }
+  }
+  const float t1 = __shfl_sync(0xffffffffu, v[0], 0);
+  const float tn = __shfl_sync(0xffffffffu, v[L - 1], 31);
+  if (mode & 2) {
+    const float sx = (t1 - p.alpha * tn) / p.den;
+#pragma unroll
+    for (int k = 0; k < L; ++k) v[k] = v[k] - sx * p.rsm[r0 + k];
+  }
+}
+
+// Padded shared-memory index: lane t reading row t*L + j hits bank
+// (t*L + j + (t*L + j)/32) mod 32, distinct over the warp for L = 4, 8, 16.
+__device__ __forceinline__ int xpad(int r) { return r + (r >> 5); }
+
+template <int L>
+__global__ void __launch_bounds__(256) rhs_fast_x(const __grid_constant__ RhsXArgs p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int line = blockIdx.x * 8 + warp;
+  if (line >= p.na) return;  // whole warps only: the shuffles stay converged
+  const int n = p.n, np = n + n / 32;
+  float* sq = reinterpret_cast<float*>(smem_raw) + (size_t)warp * 2 * np;
+  float* sa = sq + np;
+  const long long off = (long long)line * p.sa + (long long)blockIdx.y * p.sb;
+  // coalesced load of the line (u_q and u_j) into the warp's buffers
+  for (int r = lane; r < n; r += 32) {
+    sq[xpad(r)] = p.uq[off + r];
+    sa[xpad(r)] = p.ua[off + r];
+  }
+  __syncwarp();
+  const int r0 = lane * L;
+  const bool edge = (lane == 0 || lane == 31);
+  float v[L], cv[L];
+  {
+    float w[L + 4];
+#pragma unroll
+    for (int j = 0; j < L + 4; ++j) {
+      const int r = xpad(wrow(r0 - 2 + j, n, edge));
+      w[j] = sq[r] * sa[r];
+    }
+    warp_solve<K_DER1, L>(w, v, p.A, lane);
+  }
+#pragma unroll
+  for (int k = 0; k < L; ++k) cv[k] = v[k];
+  {
+    float w[L + 4];
+#pragma unroll
+    for (int j = 0; j < L + 4; ++j) w[j] = sq[xpad(wrow(r0 - 2 + j, n, edge))];
+    warp_solve<K_DER1, L>(w, v, p.B, lane);
+  }
+#pragma unroll
+  for (int k = 0; k < L; ++k) cv[k] = cv[k] + sa[xpad(r0 + k)] * v[k];
+  {
+    float w[L + 8];
+#pragma unroll
+    for (int j = 0; j < L + 8; ++j) w[j] = sq[xpad(wrow(r0 - 4 + j, n, edge))];
+    warp_solve<K_DER2, L>(w, v, p.C, lane);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < L; ++k) {
+    sq[xpad(r0 + k)] = p.nu * v[k];
+    sa[xpad(r0 + k)] = cv[k];
+  }
+  __syncwarp();
+  // coalesced store: out = (nu C + a1) + (-1/2) conv
+  float* dst = p.out + off;
+  const float* a1 = p.a1 ? p.a1 + off : nullptr;
+  for (int r = lane; r < n; r += 32) {
+    float o = sq[xpad(r)];
+    if (a1) o = o + a1[r];
+    o = o + (-0.5f) * sa[xpad(r)];
+    dst[r] = o;
+  }
+}
+
+void fill_warp_op(const OpPlan* p, WarpOp& a) {
+  const int n = p->nout;
+  const int L = n / XCH;
+  const float* dv = p->dev32;
+  a.s = dv; a.f = dv + n; a.w = dv + 2 * n; a.pf = dv + 3 * n; a.qb = dv + 4 * n; a.rsm = dv + 5 * n;
+  a.ca = (float)p->ca; a.cb = (float)p->cb; a.cc = (float)p->cc; a.cd = (float)p->cd;
+  a.alpha = (float)p->alpha;
+  a.den = (float)p->den;
+  a.nterms_int = (p->kind == K_DER2 && p->cc == 0.0 && p->cd == 0.0) ? 2 : 4;
+  const int mid = n / 2;
+  a.s_inf = (float)p->s[mid];
+  a.f_inf = (float)p->f[mid];
+  a.w_inf = (float)p->w[mid];
+  a.g_inf = (float)(-(p->f[mid] * p->w[mid]));
+  // chunk fix-up factors for chunks of L rows (the plan's are for n/16)
+  for (int c = 0; c < XCH; ++c) {
+    const int s0 = c * L, e0 = s0 + L - 1;
+    double pe = 1.0, qs = 1.0;
+    for (int r = s0; r <= e0; ++r) pe = pe * (-p->s[r]);
+    for (int r = e0; r >= s0; --r) qs = qs * (-(p->f[r] * p->w[r]));
+    a.pfe[c] = (float)pe;
+    a.qbs[c] = (float)qs;
+    bool uni = true, sm = false;
+    for (int r = s0; r <= e0; ++r) {
+      uni = uni && (float)p->s[r] == a.s_inf && (float)p->f[r] == a.f_inf && (float)p->w[r] == a.w_inf;
+      sm = sm || (float)p->rsm[r] != 0.0f;
+    }
+    a.mode[c] = (uni ? 1 : 0) | (sm ? 2 : 0);
+  }
+}
+
 template <bool XL, int L>
 int launch_rhs_k(const RhsArgs& a, dim3 grid, size_t smem, cudaStream_t st) {
   auto kern = rhs_fast<XL, L>;
@@ -217,6 +420,23 @@ int rhs_axis_fast(Ctx* c, OpPlan* pA, OpPlan* pB, OpPlan* pC, float* out, const 
   fill_fast_op(pB, a.B);
   fill_fast_op(pC, a.C);
   const bool xl = (axis == 0);
+  if (xl && n % XCH == 0 && (n / XCH == 4 || n / XCH == 8 || n / XCH == 16)) {
+    RhsXArgs x;
+    std::memset(&x, 0, sizeof(x));
+    x.ua = ua; x.uq = uq; x.a1 = a1; x.out = out;
+    x.n = n; x.na = a.na; x.sa = a.sa; x.sb = a.sb; x.nu = nu;
+    fill_warp_op(pA, x.A);
+    fill_warp_op(pB, x.B);
+    fill_warp_op(pC, x.C);
+    const dim3 g((unsigned)((a.na + 7) / 8), grid.y);
+    const int Lx = n / XCH;
+    const size_t sm = (size_t)8 * 2 * (n + n / 32) * sizeof(float);
+    if (sm > 48 * 1024) return X3D_ERR_UNSUPPORTED;
+    if (Lx == 4) rhs_fast_x<4><<<g, 256, sm, st>>>(x);
+    else if (Lx == 8) rhs_fast_x<8><<<g, 256, sm, st>>>(x);
+    else rhs_fast_x<16><<<g, 256, sm, st>>>(x);
+    return cuda_status(cudaGetLastError());
+  }
   const size_t base = (size_t)2 * FCHUNKS * LANES + 2 * LANES;
   const size_t smem = sizeof(float) * (base + (xl ? (size_t)2 * n * LD : (size_t)L * LANES * FCHUNKS));
   if (smem > 227 * 1024) return X3D_ERR_UNSUPPORTED;

@@ -560,14 +560,19 @@ static int momentum_rhs(SolverImpl* s, const T* const* u, T* const* H, cudaStrea
       RC(rc);
       RC(rhs_axis_fast(c, P[1][0], P[1][1], P[1][2], tzf, uf[1], uqf, tzf, (float)xnu, dims, st));
       s->launches += 2;
-      // x lines: the fused form needs two transposed tiles (one CTA per SM),
-      // which measured slower than the three single-solve kernels
-      Fuse<T> f = fz_prod<T>(u[q]);
-      RC(op<T>(s, 0, K_DER1, 1 - pu[0], t1, u[0], dims, st, &f));
-      f = fz_comb<T>(zero, t1, one, nullptr, zero, u[0]);
-      RC(op<T>(s, 0, K_DER1, pu[0], tg, u[q], dims, st, &f));
-      f = fz_comb<T>(xnu, tz, one, tg, mhalf, nullptr);
-      RC(op<T>(s, 0, K_DER2, pu[0], H[q], u[q], dims, st, &f));
+      if (c->grid.nx % 32 == 0 && c->grid.nx / 32 >= 4 && c->grid.nx / 32 <= 16 &&
+          (c->grid.nx / 32 & (c->grid.nx / 32 - 1)) == 0) {
+        // x lines: one warp per line (no tile)
+        RC(rhs_axis_fast(c, P[0][0], P[0][1], P[0][2], (float*)H[q], uf[0], uqf, tzf, (float)xnu, dims, st));
+        s->launches++;
+      } else {
+        Fuse<T> f = fz_prod<T>(u[q]);
+        RC(op<T>(s, 0, K_DER1, 1 - pu[0], t1, u[0], dims, st, &f));
+        f = fz_comb<T>(zero, t1, one, nullptr, zero, u[0]);
+        RC(op<T>(s, 0, K_DER1, pu[0], tg, u[q], dims, st, &f));
+        f = fz_comb<T>(xnu, tz, one, tg, mhalf, nullptr);
+        RC(op<T>(s, 0, K_DER2, pu[0], H[q], u[q], dims, st, &f));
+      }
     }
     if (fused) return cuda_status(cudaGetLastError());
   }
