@@ -11,6 +11,7 @@ with the kinetic-energy difference between the two after the same steps.
   python bench.py --workload ops [--n 512] [--ops dery,...] [--dtypes f64,f32] [--bcs 0,2]
   python bench.py --workload channel [--steps K] [--warmup W]
   python bench.py --workload les [--steps K] [--warmup W]
+  python bench.py --workload les_mlp [--n 512] [--t-end 20] [--out results.json]
 
 --impl reference times the CPU restatement of the reference's path (the
 parity oracle, C++/OpenMP on all host cores) on a bounded sample grid of the
@@ -465,9 +466,34 @@ def run_les(args):
     print(json.dumps(out), flush=True)
 
 
+def run_les_mlp(args):
+    """Learned SGS closure pipeline: TGV DNS at Re=5000 (n^3, mixed solver) ->
+    box-filtered (ratio 4) training snapshots at t = 2..10 -> MLP training ->
+    LES to t = 20 on the /4 grid with the MLP, dynamic Smagorinsky and no
+    model; dissipation errors against the filtered DNS and the step cost ratio."""
+    import incompact3d_gb300 as x3d
+    from incompact3d_gb300 import sgs
+
+    x3d.build()
+    n = args.n
+    r = sgs.run_pipeline(n_dns=n, n_les=n // 4, re=5000.0, dt=0.002, t_end=args.t_end, t_train=(2.0, 10.0),
+                         snap_every=1.0, epochs=3, batch=16384, record_every=10)
+    if args.out:
+        with open(args.out, "w") as f:
+            json.dump(r, f)
+    line = {"workload": "tgv_les_mlp_%d^3_dns_%d^3_les_re5000" % (n, n // 4), "metric": "LES dissipation error vs "
+            "filtered DNS", "unit": "relative L2 over t in [2, t_end]", "t_end": args.t_end,
+            "mlp": {k: r["mlp"][k] for k in ("eps_rel_l2", "eps_peak_rel", "ms_per_step")},
+            "dynsmag": {k: r["dynsmag"][k] for k in ("eps_rel_l2", "eps_peak_rel", "ms_per_step")},
+            "none": {k: r["none"][k] for k in ("eps_rel_l2", "eps_peak_rel", "ms_per_step")},
+            "cost_mlp_over_dynsmag": r["cost_mlp_over_dynsmag"], "r2_validation": r["r2_validation"],
+            "dns_seconds": r["dns_seconds"], "train_seconds": r["train_seconds"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "ops", "channel", "les"],
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "ops", "channel", "les", "les_mlp"],
                     help="tgv: the time-step benchmark (default); ops: operator microbench lines; "
                          "channel: the stretched turbulent channel (FP64)")
     ap.add_argument("--ops", default="", help="ops workload: comma list (derx,...,filz,poisson)")
@@ -475,6 +501,8 @@ def main():
     ap.add_argument("--bcs", default="0,2")
     ap.add_argument("--reps", type=int, default=10)
     ap.add_argument("--poisson-arith", default="fp64,double-float,fp32")
+    ap.add_argument("--t-end", type=float, default=20.0)
+    ap.add_argument("--out", default="")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
@@ -495,6 +523,8 @@ def main():
         run_channel(args)
     elif args.workload == "les":
         run_les(args)
+    elif args.workload == "les_mlp":
+        run_les_mlp(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

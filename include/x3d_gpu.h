@@ -48,6 +48,7 @@ enum {
 
 typedef struct x3d_ctx x3d_ctx;
 typedef struct x3d_solver x3d_solver;
+typedef struct x3d_mlp x3d_mlp;
 
 /* Grid: the BasicParam namelist subset (src/parameters.f90:45-90).
  * ncl: 0 periodic, 1 free-slip, 2 Dirichlet. */
@@ -332,6 +333,36 @@ int x3d_solver_set_field(x3d_solver* s, int which, const double* in, int on_devi
  * restarting so that AB3 does not repeat its Euler/AB2 start-up. */
 int x3d_solver_get_itime(x3d_solver* s);
 int x3d_solver_set_itime(x3d_solver* s, int itime);
+/* --- learned SGS closure (no counterpart in the reference; its dynamic
+ * Smagorinsky model, jles = 3, is the fallback and the cost baseline) ----------
+ * A pointwise MLP (9 velocity-gradient components du_i/dx_j, i-major, + the
+ * filter width) -> 64 -> 64 -> 6 tau_ij (xx, yy, zz, xy, xz, yz), GELU, FP32
+ * parameters.  Parameters: W1[64][10], b1[64], W2[64][64], b2[64], W3[6][64],
+ * b3[6] (x3d_mlp_param_count() floats); scales: 10 input multipliers then 6
+ * output multipliers (tau = out_scale * MLP(features * in_scale)).  Only the
+ * 10-64-64-6 shape is built. */
+int x3d_mlp_create(int nin, int nhidden, int nout, x3d_mlp** out);
+int x3d_mlp_destroy(x3d_mlp* m);
+int x3d_mlp_param_count(void);
+/* Host arrays (either may be NULL); setting resets the Adam state. */
+int x3d_mlp_set_params(x3d_mlp* m, const float* params, const float* scales);
+int x3d_mlp_get_params(x3d_mlp* m, float* params, float* scales);
+/* Y[n][6] = tau for features X[n][10] (device arrays). */
+int x3d_mlp_infer(x3d_mlp* m, const float* X, float* Y, long long n, void* stream);
+/* One Adam step (lr) on the batch X[n][10] -> T[n][6] (device arrays) with the
+ * loss mean_n sum_ij (tau/out_scale - target/out_scale)^2; loss (host, may be
+ * NULL, synchronises) receives the loss before the step. */
+int x3d_mlp_train_step(x3d_mlp* m, const float* X, const float* T, long long n, float lr, float* loss,
+                       void* stream);
+/* Box filter of ratio 4 (centred trapezoid 1/2,1,1,1,1/2 over 5 points per
+ * direction, periodic) of a fine velocity field (nx,ny,nz) onto the
+ * (nx/4,ny/4,nz/4) grid: filtered velocity and tau_ij = (u_i u_j)^f -
+ * u_i^f u_j^f (6 consecutive coarse fields in tau).  Device arrays. */
+int x3d_box_filter4(const double* ux, const double* uy, const double* uz, int nx, int ny, int nz, double* ubar,
+                    double* vbar, double* wbar, double* tau, void* stream);
+/* Use the MLP as the solver's SGS model: the force -d_j tau_ij of its
+ * stresses joins the right-hand side (FP64 solver; the model is not owned). */
+int x3d_solver_set_les_mlp(x3d_solver* s, x3d_mlp* m);
 /* Bulk velocity measured by channel_cfr (before its correction) at each
  * sub-step of the last step; returns the number of values.  Synchronises. */
 int x3d_solver_bulk_velocity(x3d_solver* s, double* out, int capacity);

@@ -124,6 +124,15 @@ def load():
         lib.x3d_get_stretching.argtypes = [P, I, P, I]
         lib.x3d_solver_set_les.argtypes = [P, I, D, D]
         lib.x3d_solver_get_field.argtypes = [P, I, P, I]
+        lib.x3d_mlp_create.argtypes = [I, I, I, ctypes.POINTER(P)]
+        lib.x3d_mlp_destroy.argtypes = [P]
+        lib.x3d_mlp_param_count.argtypes = []
+        lib.x3d_mlp_set_params.argtypes = [P, P, P]
+        lib.x3d_mlp_get_params.argtypes = [P, P, P]
+        lib.x3d_mlp_infer.argtypes = [P, P, P, LL, P]
+        lib.x3d_mlp_train_step.argtypes = [P, P, P, LL, ctypes.c_float, P, P]
+        lib.x3d_box_filter4.argtypes = [P, P, P, I, I, I, P, P, P, P, P]
+        lib.x3d_solver_set_les_mlp.argtypes = [P, P]
         lib.x3d_solver_set_field.argtypes = [P, I, P, I]
         lib.x3d_solver_get_itime.argtypes = [P]
         lib.x3d_solver_set_itime.argtypes = [P, I]

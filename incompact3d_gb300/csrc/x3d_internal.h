@@ -143,6 +143,12 @@ int poisson_010(Ctx* c, double* rhs, cudaStream_t st);
 // Device scratch of at least `bytes` bytes (contents undefined).
 int ctx_workspace(Ctx* c, size_t bytes, void** out);
 
+// Learned SGS closure (x3d_mlp.cu): tau_ij from the 9 gradient fields and the
+// filter width.
+struct Mlp;
+int mlp_les_tau(Mlp* m, const double* const* g9, double delta, double* const* tau6, long long n, int num_sms,
+                cudaStream_t st);
+
 // Device copies of a plan's vectors (made on first use).
 int upload_plan(OpPlan* p);
 // Fused momentum right-hand side along one axis on the FP32 fast path

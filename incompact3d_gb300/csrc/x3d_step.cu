@@ -450,6 +450,7 @@ struct SolverImpl {
   double* del = nullptr;      // filter width per y row (device, ny)
   x3d_ctx* cf = nullptr;      // context whose filter has alpha = 0 (dynsmag's filter(zero))
   double* lw[40] = {nullptr}; // LES work fields
+  Mlp* mlp = nullptr;         // learned closure (jles = 10), not owned
   std::vector<void*> allocs;
   ~SolverImpl() {
     for (void* p : allocs) cudaFree(p);
@@ -803,6 +804,42 @@ static int les_compute(SolverImpl* s, const double* ux, const double* uy, const 
   return cuda_status(cudaGetLastError());
 }
 
+// Learned closure: tau_ij from the MLP on the 9 velocity gradients, force
+// -d_j tau_ij into lw[LW_G..LW_G+2].
+static int les_mlp_force(SolverImpl* s, const double* ux, const double* uy, const double* uz, cudaStream_t st) {
+  Ctx* c = s->c;
+  const long long N = s->N;
+  const int dims[3] = {c->grid.nx, c->grid.ny, c->grid.nz};
+  double** w = s->lw;
+  const double* ppy = ymetric<double>(s, 0);
+  const double* U[3] = {ux, uy, uz};
+  double* g[9];
+  for (int q = 0; q < 9; ++q) g[q] = w[LW_P + q];  // slots LW_P .. LW_P+8
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      const int np = (i == j) ? 0 : 1;
+      RC(op<double>(s, j, K_DER1, np, g[3 * i + j], U[i], dims, st, nullptr, j == 1 ? ppy : nullptr));
+    }
+  double* tau[6];
+  for (int q = 0; q < 6; ++q) tau[q] = w[LW_S + q];
+  const double delta = std::cbrt(c->ax[0].d * c->ax[1].d * c->ax[2].d);
+  RC(mlp_les_tau(s->mlp, g, delta, tau, N, c->num_sms, st));
+  s->launches++;
+  // f_i = -(d_x tau_ix + d_y tau_iy + d_z tau_iz)
+  const int ti[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+  const int pt[6][3] = {{1, 1, 1}, {1, 1, 1}, {1, 1, 1}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
+  for (int i = 0; i < 3; ++i) {
+    double* G = w[LW_G + i];
+    for (int j = 0; j < 3; ++j) {
+      const int q = ti[i][j];
+      // G = -d_j tau_ij (+ G)
+      Fuse<double> f = fz_comb<double>(-1.0, j == 0 ? nullptr : G, 1.0, nullptr, 0.0, nullptr);
+      RC(op<double>(s, j, K_DER1, pt[q][j], G, tau[q], dims, st, &f, j == 1 ? ppy : nullptr));
+    }
+  }
+  return cuda_status(cudaGetLastError());
+}
+
 // ppy as channel_cfr divides by it: the stretching metric, or on a uniform
 // mesh the default 1 with 2 at the walls (src/variables.f90:1294-1305).
 static const double* ymetric_cfr(SolverImpl* s) {
@@ -834,7 +871,11 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
   RC(momentum_rhs<T>(s, u, H, st));
   if (s->jles != 0) {
     // src/transeq.f90:475-480: the SGS force joins the right-hand side
-    RC(les_compute(s, s->ux, s->uy, s->uz, st));
+    if (s->jles == 10) {
+      RC(les_mlp_force(s, s->ux, s->uy, s->uz, st));
+    } else {
+      RC(les_compute(s, s->ux, s->uy, s->uz, st));
+    }
     k_add3<<<nb, 256, 0, st>>>((double*)H[0], (double*)H[1], (double*)H[2], s->lw[LW_G], s->lw[LW_G + 1],
                                s->lw[LW_G + 2], N);
     s->launches++;
@@ -1069,12 +1110,33 @@ int x3d_solver_set_les(x3d_solver* s, int jles, double smagcst, double maxdsmagc
   return X3D_OK;
 }
 
+int x3d_solver_set_les_mlp(x3d_solver* s, x3d_mlp* m) {
+  if (!s) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  if (!m) {
+    si->mlp = nullptr;
+    if (si->jles == 10) si->jles = 0;
+    return X3D_OK;
+  }
+  int rc = x3d_solver_set_les(s, 1, si->smagcst, si->maxdsmagcst);  // work fields and filter width
+  if (rc != X3D_OK) return rc;
+  si->mlp = reinterpret_cast<Mlp*>(m);
+  si->jles = 10;
+  return X3D_OK;
+}
+
 int x3d_solver_les_fields(x3d_solver* s, double* nut, double* sgsx, double* sgsy, double* sgsz, void* stream) {
   if (!s || !nut || !sgsx || !sgsy || !sgsz) return X3D_ERR_ARG;
   SolverImpl* si = &s->impl;
   if (si->jles == 0) return X3D_ERR_STATE;
   cudaStream_t st = (cudaStream_t)stream;
-  int rc = les_compute(si, si->ux, si->uy, si->uz, st);
+  int rc = X3D_OK;
+  if (si->jles == 10) {
+    rc = les_mlp_force(si, si->ux, si->uy, si->uz, st);
+    if (rc == X3D_OK) rc = cuda_status(cudaMemsetAsync(si->lw[LW_NUT], 0, (size_t)si->N * sizeof(double), st));
+  } else {
+    rc = les_compute(si, si->ux, si->uy, si->uz, st);
+  }
   if (rc != X3D_OK) return rc;
   const size_t b = (size_t)si->N * sizeof(double);
   double* dst[4] = {nut, sgsx, sgsy, sgsz};
