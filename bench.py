@@ -467,7 +467,8 @@ def run_les(args):
 
 
 def run_les_mlp(args):
-    """Learned SGS closure pipeline: TGV DNS at Re=5000 (n^3, mixed solver) ->
+    """Learned SGS closure pipeline: TGV DNS at Re=5000 (n^3, mixed solver,
+    dt = 0.001; dt = 0.002 diverged near t = 7.3 at 512^3 with AB3) ->
     box-filtered (ratio 4) training snapshots at t = 2..10 -> MLP training ->
     LES to t = 20 on the /4 grid with the MLP, dynamic Smagorinsky and no
     model; dissipation errors against the filtered DNS and the step cost ratio."""
@@ -476,8 +477,10 @@ def run_les_mlp(args):
 
     x3d.build()
     n = args.n
-    r = sgs.run_pipeline(n_dns=n, n_les=n // 4, re=5000.0, dt=0.002, t_end=args.t_end, t_train=(2.0, 10.0),
-                         snap_every=1.0, epochs=3, batch=16384, record_every=10)
+    r = sgs.run_pipeline(n_dns=n, n_les=n // 4, re=5000.0, dt=0.002, dt_dns=0.001, t_end=args.t_end,
+                         t_train=(2.0, 10.0), snap_every=1.0, epochs=args.epochs, batch=16384, record_every=10,
+                         flux_lambda=args.flux_lambda, data_in=args.data_in or None,
+                         data_out=args.data_out or None)
     if args.out:
         with open(args.out, "w") as f:
             json.dump(r, f)
@@ -487,6 +490,7 @@ def run_les_mlp(args):
             "dynsmag": {k: r["dynsmag"][k] for k in ("eps_rel_l2", "eps_peak_rel", "ms_per_step")},
             "none": {k: r["none"][k] for k in ("eps_rel_l2", "eps_peak_rel", "ms_per_step")},
             "cost_mlp_over_dynsmag": r["cost_mlp_over_dynsmag"], "r2_validation": r["r2_validation"],
+            "flux_ratio_validation": r["flux_ratio_validation"], "flux_lambda": r["flux_lambda"],
             "dns_seconds": r["dns_seconds"], "train_seconds": r["train_seconds"]}
     print(json.dumps(line), flush=True)
 
@@ -503,6 +507,10 @@ def main():
     ap.add_argument("--poisson-arith", default="fp64,double-float,fp32")
     ap.add_argument("--t-end", type=float, default=20.0)
     ap.add_argument("--out", default="")
+    ap.add_argument("--epochs", type=int, default=3)
+    ap.add_argument("--flux-lambda", type=float, default=1.0)
+    ap.add_argument("--data-in", default="")
+    ap.add_argument("--data-out", default="")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)

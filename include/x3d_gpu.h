@@ -354,6 +354,10 @@ int x3d_mlp_infer(x3d_mlp* m, const float* X, float* Y, long long n, void* strea
  * NULL, synchronises) receives the loss before the step. */
 int x3d_mlp_train_step(x3d_mlp* m, const float* X, const float* T, long long n, float lr, float* loss,
                        void* stream);
+/* Add lam * ((Pi_model - Pi_target) / pscale)^2 to the training loss, with the
+ * subgrid energy flux Pi = tau_ij S_ij (S from the raw gradient features);
+ * lam = 0 (default) is the plain stress loss. */
+int x3d_mlp_set_flux_loss(x3d_mlp* m, float lam, float pscale);
 /* Box filter of ratio 4 (centred trapezoid 1/2,1,1,1,1/2 over 5 points per
  * direction, periodic) of a fine velocity field (nx,ny,nz) onto the
  * (nx/4,ny/4,nz/4) grid: filtered velocity and tau_ij = (u_i u_j)^f -

@@ -113,8 +113,11 @@ __global__ void __launch_bounds__(256) k_mlp_les(const float* P, const float* sc
 constexpr int TB = 64;
 constexpr int PD = TB + 1;
 
+// Optional energy-flux term of the loss: lam * ((Pi_model - Pi_data) / pscale)^2
+// with Pi = tau_ij S_ij (S from the raw gradient features), which ties the
+// model to the subgrid dissipation the LES needs.
 __global__ void __launch_bounds__(TB) k_mlp_grad(const float* P, const float* sc, const float* X, const float* T,
-                                                 long long n, float* part, float* lpart) {
+                                                 long long n, float lam, float pscale, float* part, float* lpart) {
   extern __shared__ float sm[];
   float* sp = sm;                  // parameters + scales
   float* xs = sp + NPAR + NI + NO;  // [NI][PD]
@@ -156,15 +159,34 @@ __global__ void __launch_bounds__(TB) k_mlp_grad(const float* P, const float* sc
 #pragma unroll
     for (int m = 0; m < NO; ++m) y[m] = y[m] + sp[OW3 + m * NH + j] * g;
   }
-  // loss: mean over the batch of sum_m (y_m - t_m / outscale_m)^2
+  // loss: mean over the batch of sum_m (y_m - t_m / outscale_m)^2 [+ flux term]
   float dy[NO], l = 0.f;
 #pragma unroll
   for (int m = 0; m < NO; ++m) {
     const float e = ok ? y[m] - T[s * NO + m] / outsc[m] : 0.f;
     l = l + e * e;
     dy[m] = 2.f * e / (float)n;
-    dys[m * PD + t] = dy[m];
   }
+  if (lam != 0.f && ok) {
+    const float* g = X + s * NI;  // raw du_i/dx_j, i-major
+    const float S[NO] = {g[0], g[4], g[8], 0.5f * (g[1] + g[3]), 0.5f * (g[2] + g[6]), 0.5f * (g[5] + g[7])};
+    float pm = 0.f, pd = 0.f;
+#pragma unroll
+    for (int m = 0; m < NO; ++m) {
+      const float wm = (m < 3) ? 1.f : 2.f;
+      pm = pm + wm * (y[m] * outsc[m]) * S[m];
+      pd = pd + wm * T[s * NO + m] * S[m];
+    }
+    const float e = (pm - pd) / pscale;
+    l = l + lam * e * e;
+#pragma unroll
+    for (int m = 0; m < NO; ++m) {
+      const float wm = (m < 3) ? 1.f : 2.f;
+      dy[m] = dy[m] + 2.f * lam * e * wm * S[m] * outsc[m] / pscale / (float)n;
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < NO; ++m) dys[m * PD + t] = dy[m];
   ls[t] = l;
   for (int j = 0; j < NH; ++j) {
     float d = 0.f;
@@ -282,6 +304,7 @@ struct Mlp {
   float* lsum = nullptr;
   int nbmax = 0;
   int step = 0;
+  float lam = 0.f, pscale = 1.f;  // energy-flux loss term
   ~Mlp() {
     for (float* p : {P, m1, m2, sc, part, lpart, lsum})
       if (p) cudaFree(p);
@@ -393,7 +416,7 @@ int x3d_mlp_train_step(x3d_mlp* h, const float* X, const float* T, long long n, 
     if (e != cudaSuccess) return cuda_status(e);
     configured = true;
   }
-  k_mlp_grad<<<nb, TB, smem, st>>>(m->P, m->sc, X, T, n, m->part, m->lpart);
+  k_mlp_grad<<<nb, TB, smem, st>>>(m->P, m->sc, X, T, n, m->lam, m->pscale, m->part, m->lpart);
   m->step += 1;
   const float b1c = 1.f - powf(0.9f, (float)m->step), b2c = 1.f - powf(0.999f, (float)m->step);
   k_mlp_adam<<<(NPAR + 255) / 256, 256, 0, st>>>(m->P, m->m1, m->m2, m->part, nb, lr, b1c, b2c);
@@ -405,6 +428,14 @@ int x3d_mlp_train_step(x3d_mlp* h, const float* X, const float* T, long long n, 
     *loss = hl / (float)n;
   }
   return cuda_status(cudaGetLastError());
+}
+
+int x3d_mlp_set_flux_loss(x3d_mlp* h, float lam, float pscale) {
+  if (!h || !(pscale > 0.f) || lam < 0.f) return X3D_ERR_ARG;
+  Mlp* m = reinterpret_cast<Mlp*>(h);
+  m->lam = lam;
+  m->pscale = pscale;
+  return X3D_OK;
 }
 
 int x3d_box_filter4(const double* ux, const double* uy, const double* uz, int nx, int ny, int nz, double* ubar,

@@ -63,6 +63,12 @@ class Mlp:
                                           s.ctypes.data_as(ctypes.c_void_p)), "x3d_mlp_get_params")
         return p, s
 
+    def set_flux_loss(self, lam, pscale):
+        """Add lam * ((Pi_model - Pi_data) / pscale)^2 to the training loss,
+        Pi = tau_ij S_ij the subgrid energy flux of a sample."""
+        check(self.lib.x3d_mlp_set_flux_loss(self.h, ctypes.c_float(lam), ctypes.c_float(pscale)),
+              "x3d_mlp_set_flux_loss")
+
     def infer(self, X):
         torch = _torch()
         Y = torch.empty((X.shape[0], NOUT), dtype=torch.float32, device=X.device)
@@ -129,28 +135,27 @@ def _stats(torch, s):
     return e
 
 
-def run_pipeline(n_dns=512, n_les=128, re=5000.0, dt=0.002, t_end=20.0, t_train=(2.0, 10.0), snap_every=1.0,
-                 epochs=3, batch=16384, lr=1e-3, record_every=10, seed=0, log=print):
-    """DNS -> box-filtered training set -> MLP training -> LES comparison.
-
-    Returns a dict: filtered-DNS and LES kinetic energy / dissipation histories,
-    the dissipation errors of the learned and the dynamic-Smagorinsky LES
-    against the filtered DNS, step costs, and the training / validation loss."""
+def dns_dataset(n_dns=512, n_les=128, re=5000.0, dt=0.002, dt_dns=None, t_end=20.0, t_train=(2.0, 10.0),
+                snap_every=1.0, record_every=10):
+    """Run the DNS (mixed-precision solver) and return the box-filtered data:
+    training snapshots (all but the last) and validation snapshot (the last)
+    as feature / target arrays on the device, and the filtered kinetic energy
+    history at every record_every LES steps."""
     torch = _torch()
     L = 2 * math.pi
     xnu = 1.0 / re
     lib = _lib.load()
-    out = {"n_dns": n_dns, "n_les": n_les, "re": re, "dt": dt, "t_end": t_end}
-    # ---- DNS with box-filtered statistics and training snapshots ----------
+    dt_dns = dt if dt_dns is None else dt_dns
+    sub = int(round(dt / dt_dns))
     cd = Context(n_dns, n_dns, n_dns, L, L, L)
     cl = Context(n_les, n_les, n_les, L, L, L)
-    sd = Solver(cd, dt, xnu, itimescheme=3, precision=_lib.PREC_MIXED)
+    sd = Solver(cd, dt_dns, xnu, itimescheme=3, precision=_lib.PREC_MIXED)
     sd.init_tgv()
-    shp = (n_dns, n_dns, n_dns)
-    u = [torch.empty(shp, dtype=torch.float64, device="cuda") for _ in range(3)]
+    u = [torch.empty((n_dns,) * 3, dtype=torch.float64, device="cuda") for _ in range(3)]
     nsteps = int(round(t_end / dt))
     snaps = set(int(round(t / dt)) for t in np.arange(t_train[0], t_train[1] + 1e-9, snap_every))
     Xs, Ts, tdns, edns = [], [], [], []
+    delta = None
     t0 = time.time()
     for it in range(0, nsteps + 1):
         if it % record_every == 0 or it in snaps:
@@ -164,21 +169,55 @@ def run_pipeline(n_dns=512, n_les=128, re=5000.0, dt=0.002, t_end=20.0, t_train=
                 Xs.append(X)
                 Ts.append(tau.reshape(6, -1).t().contiguous().float())
         if it < nsteps:
-            sd.step(1)
+            sd.step(sub)
     torch.cuda.synchronize()
-    out["dns_seconds"] = time.time() - t0
+    secs = time.time() - t0
     sd.close()
-    del u
-    # ---- training ------------------------------------------------------------
-    Xtr = torch.cat(Xs[:-1]) if len(Xs) > 1 else Xs[0]
-    Ttr = torch.cat(Ts[:-1]) if len(Ts) > 1 else Ts[0]
-    Xva, Tva = Xs[-1], Ts[-1]
+    if not all(np.isfinite(edns)):
+        raise FloatingPointError("the DNS diverged (filtered kinetic energy not finite)")
+    return {"Xtr": torch.cat(Xs[:-1]), "Ttr": torch.cat(Ts[:-1]), "Xva": Xs[-1], "Tva": Ts[-1], "delta": delta,
+            "t": np.array(tdns), "E": np.array(edns), "dns_seconds": secs}
+
+
+def save_dataset(path, d, ntrain=600_000, nval=150_000, seed=0):
+    """A random subsample of the box-filtered data (features, targets) and the
+    filtered kinetic-energy history, as an .npz file."""
+    torch = _torch()
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    it = torch.randperm(d["Xtr"].shape[0], device="cuda", generator=g)[:ntrain]
+    iv = torch.randperm(d["Xva"].shape[0], device="cuda", generator=g)[:nval]
+    np.savez(path, Xtr=d["Xtr"][it].cpu().numpy(), Ttr=d["Ttr"][it].cpu().numpy(), Xva=d["Xva"][iv].cpu().numpy(),
+             Tva=d["Tva"][iv].cpu().numpy(), delta=d["delta"], t=d["t"], E=d["E"])
+
+
+def load_dataset(path):
+    torch = _torch()
+    z = np.load(path)
+    return {"Xtr": torch.from_numpy(z["Xtr"]).cuda(), "Ttr": torch.from_numpy(z["Ttr"]).cuda(),
+            "Xva": torch.from_numpy(z["Xva"]).cuda(), "Tva": torch.from_numpy(z["Tva"]).cuda(),
+            "delta": float(z["delta"]), "t": z["t"], "E": z["E"], "dns_seconds": 0.0}
+
+
+def flux(X, T):
+    """Subgrid energy flux tau_ij S_ij of samples (raw gradient features)."""
+    S = [X[:, 0], X[:, 4], X[:, 8], 0.5 * (X[:, 1] + X[:, 3]), 0.5 * (X[:, 2] + X[:, 6]), 0.5 * (X[:, 5] + X[:, 7])]
+    w = [1.0, 1.0, 1.0, 2.0, 2.0, 2.0]
+    return sum(w[m] * T[:, m] * S[m] for m in range(6))
+
+
+def train(d, epochs=3, batch=16384, lr=1e-3, flux_lambda=1.0, seed=0):
+    """Train the MLP on the dataset; returns (model, log dict)."""
+    torch = _torch()
+    Xtr, Ttr = d["Xtr"], d["Ttr"]
     insc = np.ones(NIN, np.float32)
     insc[:9] = 1.0 / Xtr[:, :9].std(dim=0).clamp_min(1e-30).cpu().numpy()
-    insc[9] = 1.0 / delta
+    insc[9] = 1.0 / d["delta"]
     outsc = Ttr.std(dim=0).clamp_min(1e-30).cpu().numpy().astype(np.float32)
     mlp = Mlp(seed)
     mlp.set(init_params(seed), np.concatenate([insc, outsc]))
+    pscale = float(flux(Xtr, Ttr).std())
+    mlp.set_flux_loss(flux_lambda, pscale)
     g = torch.Generator(device="cuda")
     g.manual_seed(seed)
     nb = Xtr.shape[0] // batch
@@ -196,18 +235,28 @@ def run_pipeline(n_dns=512, n_les=128, re=5000.0, dt=0.002, t_end=20.0, t_train=
                 losses.append((step, lv))
             step += 1
     torch.cuda.synchronize()
-    out["train_seconds"] = time.time() - t0
-    out["train_loss"] = losses
 
-    def val_r2(X, T):
+    def r2(X, T):
         Y = mlp.infer(X)
         r = ((Y - T) ** 2).sum(dim=0) / ((T - T.mean(dim=0)) ** 2).sum(dim=0)
-        return [float(1 - v) for v in r.cpu()]
+        pf, tf = flux(X, Y), flux(X, T)
+        return [float(1 - v) for v in r.cpu()], float(pf.mean() / tf.mean())
 
-    out["r2_train"] = val_r2(Xtr[: min(Xtr.shape[0], 2_000_000)], Ttr[: min(Xtr.shape[0], 2_000_000)])
-    out["r2_validation"] = val_r2(Xva, Tva)
-    del Xs, Ts, Xtr, Ttr
-    # ---- LES runs -------------------------------------------------------------
+    m = min(Xtr.shape[0], 2_000_000)
+    r2t, ft = r2(Xtr[:m], Ttr[:m])
+    r2v, fv = r2(d["Xva"], d["Tva"])
+    return mlp, {"train_seconds": time.time() - t0, "train_loss": losses, "r2_train": r2t, "r2_validation": r2v,
+                 "flux_ratio_train": ft, "flux_ratio_validation": fv, "flux_lambda": flux_lambda}
+
+
+def les_compare(mlp, d, n_les=128, re=5000.0, dt=0.002, t_end=20.0, t_from=2.0, record_every=10):
+    """LES runs (MLP, dynamic Smagorinsky, no model) against the filtered DNS."""
+    torch = _torch()
+    L = 2 * math.pi
+    xnu = 1.0 / re
+    lib = _lib.load()
+    cl = Context(n_les, n_les, n_les, L, L, L)
+    nsteps = int(round(t_end / dt))
     runs = {}
     for name in ("mlp", "dynsmag", "none"):
         s = Solver(cl, dt, xnu, itimescheme=3, precision=_lib.PREC_FP64)
@@ -233,17 +282,15 @@ def run_pipeline(n_dns=512, n_les=128, re=5000.0, dt=0.002, t_end=20.0, t_train=
                 tstep += ev0.elapsed_time(ev1)
         runs[name] = {"E": es, "ms_per_step": tstep / max(1, nsteps)}
         s.close()
-    tt = np.array(tdns)
-    ef = np.array(edns)
+    tt = np.asarray(d["t"])
+    ef = np.asarray(d["E"])
 
     def diss(e):
         return -np.gradient(np.asarray(e), tt)
 
     epsf = diss(ef)
-    win = tt >= t_train[0]
-    out["t"] = tt.tolist()
-    out["E_filtered_dns"] = ef.tolist()
-    out["eps_filtered_dns"] = epsf.tolist()
+    win = tt >= t_from
+    out = {"t": tt.tolist(), "E_filtered_dns": ef.tolist(), "eps_filtered_dns": epsf.tolist()}
     for name, r in runs.items():
         eps = diss(r["E"])
         r["eps"] = eps.tolist()
@@ -251,6 +298,26 @@ def run_pipeline(n_dns=512, n_les=128, re=5000.0, dt=0.002, t_end=20.0, t_train=
         r["eps_peak_rel"] = float(abs(eps[win].max() - epsf[win].max()) / epsf[win].max())
         out[name] = r
     out["cost_mlp_over_dynsmag"] = runs["mlp"]["ms_per_step"] / runs["dynsmag"]["ms_per_step"]
+    return out
+
+
+def run_pipeline(n_dns=512, n_les=128, re=5000.0, dt=0.002, dt_dns=None, t_end=20.0, t_train=(2.0, 10.0),
+                 snap_every=1.0, epochs=3, batch=16384, lr=1e-3, flux_lambda=1.0, record_every=10, seed=0,
+                 data_in=None, data_out=None):
+    """DNS -> box-filtered training set -> MLP training -> LES comparison.
+    data_in: load a saved dataset instead of running the DNS; data_out: save a
+    subsample of the DNS data for later runs."""
+    if data_in:
+        d = load_dataset(data_in)
+    else:
+        d = dns_dataset(n_dns, n_les, re, dt, dt_dns, t_end, t_train, snap_every, record_every)
+        if data_out:
+            save_dataset(data_out, d, seed=seed)
+    mlp, log = train(d, epochs, batch, lr, flux_lambda, seed)
+    out = {"n_dns": n_dns, "n_les": n_les, "re": re, "dt": dt, "dt_dns": dt_dns, "t_end": t_end,
+           "dns_seconds": d["dns_seconds"]}
+    out.update(log)
+    out.update(les_compare(mlp, d, n_les, re, dt, t_end, t_train[0], record_every))
     out["params"], out["scales"] = [a.tolist() for a in mlp.get()]
     mlp.close()
     return out

@@ -33,13 +33,20 @@ def np_forward(P, sc, X):
     return x, a1, h1, a2, h2, y
 
 
-def np_grad(P, sc, X, T):
+def np_grad(P, sc, X, T, lam=0.0, pscale=1.0):
     x, a1, h1, a2, h2, y = np_forward(P, sc, X)
     n = X.shape[0]
     W2 = P[704:4800].reshape(64, 64)
     W3 = P[4864:5248].reshape(6, 64)
     gd = lambda a: 0.5 * (1 + erf(a / math.sqrt(2))) + a * np.exp(-0.5 * a * a) / math.sqrt(2 * math.pi)  # noqa
     dy = 2 * (y - T / sc[10:]) / n
+    if lam:
+        # energy flux Pi = tau_ij S_ij with S from the raw gradient features
+        S = np.stack([X[:, 0], X[:, 4], X[:, 8], 0.5 * (X[:, 1] + X[:, 3]), 0.5 * (X[:, 2] + X[:, 6]),
+                      0.5 * (X[:, 5] + X[:, 7])], axis=1)
+        w = np.array([1, 1, 1, 2, 2, 2.0])
+        e = ((y * sc[10:] * w * S).sum(1) - (T * w * S).sum(1)) / pscale
+        dy = dy + 2 * lam * e[:, None] * w * S * sc[10:] / pscale / n
     d2 = (dy @ W3) * gd(a2)
     d1 = (d2 @ W2) * gd(a1)
     return np.concatenate([(d1.T @ x).ravel(), d1.sum(0), (d2.T @ h1).ravel(), d2.sum(0), (dy.T @ h2).ravel(),
@@ -81,6 +88,31 @@ def test_first_adam_step_follows_gradient_sign(mlp):
     step = P1 - P0
     assert np.all(np.sign(step[big]) == -np.sign(g[big]))
     np.testing.assert_allclose(np.abs(step[big]), 1e-3, rtol=1e-2)
+
+
+def test_first_adam_step_with_flux_loss(mlp):
+    import torch
+    P0, sc = mlp.get()
+    rng = np.random.default_rng(9)
+    X = rng.standard_normal((3000, 10)).astype(np.float32)
+    T = rng.standard_normal((3000, 6)).astype(np.float32)
+    mlp.set_flux_loss(2.0, 3.0)
+    mlp.train_step(torch.from_numpy(X).cuda(), torch.from_numpy(T).cuda(), 1e-3)
+    P1, _ = mlp.get()
+    g = np_grad(P0.astype(np.float64), sc.astype(np.float64), X.astype(np.float64), T.astype(np.float64), 2.0, 3.0)
+    g0 = np_grad(P0.astype(np.float64), sc.astype(np.float64), X.astype(np.float64), T.astype(np.float64))
+    big = np.abs(g) > 1e-4 * np.abs(g).max()
+    step = P1 - P0
+    assert np.all(np.sign(step[big]) == -np.sign(g[big]))
+    # the flux term changes the direction of a share of the parameters
+    assert np.mean(np.sign(g[big]) != np.sign(g0[big])) > 0.05
+
+
+def test_flux_loss_rejects_bad_arguments(mlp):
+    with pytest.raises(Exception):
+        mlp.set_flux_loss(1.0, 0.0)
+    with pytest.raises(Exception):
+        mlp.set_flux_loss(-1.0, 1.0)
 
 
 def test_training_fits_a_smooth_map(mlp):
