@@ -356,6 +356,24 @@ def run_ops(args):
                       flush=True)
             del u, o
         del ctx, f64
+    cd = [a for a in ("convdiffx", "convdiffy", "convdiffz") if want is None or a in want]
+    if cd:
+        # fused momentum term of one direction (FP32, periodic): reads u_j,
+        # u_q and the running sum, writes the result -> 4 N * 4 bytes
+        ctx = x3d.Context(n, n, n, L, L, L)
+        uj = spectral_field(torch, n, L, True, seed=1).float()
+        uq = spectral_field(torch, n, L, True, seed=2).float()
+        a1 = spectral_field(torch, n, L, True, seed=3).float()
+        o = torch.empty_like(uq)
+        for nm in cd:
+            axis = "xyz".index(nm[-1])
+            sec = time_kernel(torch, lambda: ctx.conv_diff(axis, 1, uj, uq, a1, 1 / 1600.0, out=o), args.reps,
+                              stream)
+            gbs = 4 * N * 4 / sec / 1e9
+            print(json.dumps({"op": nm, "dtype": "f32", "ncl": 0, "n": n, "ms": round(1e3 * sec, 4),
+                              "gbs": round(gbs, 1), "frac": round(gbs / pk, 4), "peak_source": pk_kind}),
+                  flush=True)
+        del ctx, uj, uq, a1, o
     if want is None or "poisson" in want:
         ctx = x3d.Context(n, n, n, L, L, L)
         rhs0 = spectral_field(torch, n, L, True, zero_mean=True)

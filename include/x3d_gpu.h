@@ -190,6 +190,22 @@ int x3d_interzpv(x3d_ctx* ctx, double* tz, const double* uz, double* rz, double*
 int x3d_apply(x3d_ctx* ctx, int axis, int op, int npaire, int coefset, int dtype, void* t, const void* u,
               const int* dims_in, void* stream);
 
+/* One direction's share of the momentum right-hand side of component u_q,
+ * binary32, periodic lines (src/transeq.f90:73-591: the convective term in
+ * skew-symmetric form plus the viscous term along axis j = axis):
+ *   out = nu d_jj u_q + a1 - (d_j(u_j u_q) + u_j d_j u_q) / 2
+ * npaire is (q == axis ? 0 : 1) for d_j u_q and d_jj u_q and the reverse for
+ * the product, as momentum_rhs_eq calls them.  The three solves of a line run
+ * in one kernel, reading u_j, u_q and a1 once and writing out once.  a1 may be
+ * null (zero) or alias out.  dims = (nx, ny, nz) of the context.  Returns
+ * X3D_ERR_UNSUPPORTED where the fused kernel does not apply: a non-periodic
+ * axis, a stretched y axis, or a line length other than 16 * {8, 16, 32}
+ * (32 * {4, 8, 16} also for x).  No reference counterpart as one call: it
+ * replaces the derx/dery/derz + derxx/deryy/derzz sequence of one direction in
+ * momentum_rhs_eq. */
+int x3d_conv_diff_f32(x3d_ctx* ctx, int axis, int q, float* out, const float* uj, const float* uq,
+                      const float* a1, float nu, const int* dims, void* stream);
+
 /* Host-side description of the plan x3d_apply uses for (axis, op, npaire,
  * coefset): the line kernel's interior coefficients, Thomas factors,
  * chunked-solve fix-up factors, Sherman-Morrison vector and boundary-row

@@ -88,6 +88,7 @@ def load():
         lib.x3d_get_coeffs.argtypes = [P, I, I, P, I]
         lib.x3d_apply.argtypes = [P, I, I, I, I, I, P, P, P, P]
         lib.x3d_plan_info.argtypes = [P, I, I, I, I, P, P, P]
+        lib.x3d_conv_diff_f32.argtypes = [P, I, I, P, P, P, P, ctypes.c_float, P, P]
         colloc = [P, P, P, P, P, P, P, P, I, I, I, I, D, P]
         for n in ("derx", "derz", "derxx", "deryy", "derzz", "filx", "fily", "filz"):
             getattr(lib, "x3d_" + n).argtypes = colloc

@@ -274,6 +274,21 @@ int x3d_apply(x3d_ctx* h, int axis, int op, int npaire, int coefset, int dtype, 
   return X3D_ERR_DTYPE;
 }
 
+int x3d_conv_diff_f32(x3d_ctx* h, int axis, int q, float* out, const float* uj, const float* uq, const float* a1,
+                      float nu, const int* dims, void* st) {
+  if (!h || !out || !uj || !uq || !dims || axis < 0 || axis > 2 || q < 0 || q > 2) return X3D_ERR_ARG;
+  Ctx* c = C(h);
+  if (dims[0] != c->grid.nx || dims[1] != c->grid.ny || dims[2] != c->grid.nz) return X3D_ERR_SHAPE;
+  if (axis == 1 && c->st.istret != 0) return X3D_ERR_UNSUPPORTED;
+  const int pu = (q == axis) ? 0 : 1;  // parity of d_j u_q (momentum_rhs_eq's npaire)
+  OpPlan *pA = nullptr, *pB = nullptr, *pC = nullptr;
+  int rc = get_plan(c, axis, K_DER1, 1 - pu, default_coefset(K_DER1, 1 - pu), &pA);
+  if (rc == X3D_OK) rc = get_plan(c, axis, K_DER1, pu, default_coefset(K_DER1, pu), &pB);
+  if (rc == X3D_OK) rc = get_plan(c, axis, K_DER2, pu, default_coefset(K_DER2, pu), &pC);
+  if (rc != X3D_OK) return rc;
+  return rhs_axis_fast(c, pA, pB, pC, out, uj, uq, a1, nu, dims, (cudaStream_t)st);
+}
+
 int x3d_plan_info(x3d_ctx* h, int axis, int op, int npaire, int coefset, double* scalars, double* vecs,
                   double* brows) {
   if (!h) return X3D_ERR_ARG;

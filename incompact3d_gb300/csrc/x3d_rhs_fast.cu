@@ -277,21 +277,54 @@ __device__ __forceinline__ void warp_solve(const float* w, float* v, const WarpO
 // (t*L + j + (t*L + j)/32) mod 32, distinct over the warp for L = 4, 8, 16.
 __device__ __forceinline__ int xpad(int r) { return r + (r >> 5); }
 
+// Asynchronous 4-byte global -> shared copy (LDGSTS): the copies of a whole
+// line are in flight at once and hold no registers.
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
+}
+
+// Shared memory per warp: u_q, u_j and the running sum a1, each a padded line.
 template <int L>
-__global__ void __launch_bounds__(256) rhs_fast_x(const __grid_constant__ RhsXArgs p) {
+__host__ __device__ constexpr int xline_pad() {
+  return 32 * L + L;
+}
+
+template <int L>
+__global__ void __launch_bounds__(256, 3) rhs_fast_x(const __grid_constant__ RhsXArgs p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int N = 32 * L, NP = xline_pad<L>();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int line = blockIdx.x * 8 + warp;
   if (line >= p.na) return;  // whole warps only: the shuffles stay converged
-  const int n = p.n, np = n + n / 32;
-  float* sq = reinterpret_cast<float*>(smem_raw) + (size_t)warp * 2 * np;
-  float* sa = sq + np;
+  float* sq = reinterpret_cast<float*>(smem_raw) + (size_t)warp * 3 * NP;
+  float* sa = sq + NP;
+  float* s1 = sa + NP;
   const long long off = (long long)line * p.sa + (long long)blockIdx.y * p.sb;
-  // coalesced load of the line (u_q and u_j) into the warp's buffers
-  for (int r = lane; r < n; r += 32) {
-    sq[xpad(r)] = p.uq[off + r];
-    sa[xpad(r)] = p.ua[off + r];
+  // line r = lane + 32 i goes to padded row r + i; group 0 = u_q and u_j,
+  // group 1 = a1 (waited for only before the store)
+  {
+    const float* gq = p.uq + off;
+    const float* ga = p.ua + off;
+#pragma unroll
+    for (int i = 0; i < L; ++i) {
+      cp_async4(sq + lane + 33 * i, gq + lane + 32 * i);
+      cp_async4(sa + lane + 33 * i, ga + lane + 32 * i);
+    }
+    cp_async_commit();
+    if (p.a1) {
+      const float* g1 = p.a1 + off;
+#pragma unroll
+      for (int i = 0; i < L; ++i) cp_async4(s1 + lane + 33 * i, g1 + lane + 32 * i);
+    }
+    cp_async_commit();
   }
+  cp_async_wait<1>();
   __syncwarp();
   const int r0 = lane * L;
   const bool edge = (lane == 0 || lane == 31);
@@ -300,7 +333,7 @@ __global__ void __launch_bounds__(256) rhs_fast_x(const __grid_constant__ RhsXAr
     float w[L + 4];
 #pragma unroll
     for (int j = 0; j < L + 4; ++j) {
-      const int r = xpad(wrow(r0 - 2 + j, n, edge));
+      const int r = xpad(wrow(r0 - 2 + j, N, edge));
       w[j] = sq[r] * sa[r];
     }
     warp_solve<K_DER1, L>(w, v, p.A, lane);
@@ -310,7 +343,7 @@ __global__ void __launch_bounds__(256) rhs_fast_x(const __grid_constant__ RhsXAr
   {
     float w[L + 4];
 #pragma unroll
-    for (int j = 0; j < L + 4; ++j) w[j] = sq[xpad(wrow(r0 - 2 + j, n, edge))];
+    for (int j = 0; j < L + 4; ++j) w[j] = sq[xpad(wrow(r0 - 2 + j, N, edge))];
     warp_solve<K_DER1, L>(w, v, p.B, lane);
   }
 #pragma unroll
@@ -318,9 +351,10 @@ __global__ void __launch_bounds__(256) rhs_fast_x(const __grid_constant__ RhsXAr
   {
     float w[L + 8];
 #pragma unroll
-    for (int j = 0; j < L + 8; ++j) w[j] = sq[xpad(wrow(r0 - 4 + j, n, edge))];
+    for (int j = 0; j < L + 8; ++j) w[j] = sq[xpad(wrow(r0 - 4 + j, N, edge))];
     warp_solve<K_DER2, L>(w, v, p.C, lane);
   }
+  cp_async_wait<0>();
   __syncwarp();
 #pragma unroll
   for (int k = 0; k < L; ++k) {
@@ -330,12 +364,14 @@ __global__ void __launch_bounds__(256) rhs_fast_x(const __grid_constant__ RhsXAr
   __syncwarp();
   // coalesced store: out = (nu C + a1) + (-1/2) conv
   float* dst = p.out + off;
-  const float* a1 = p.a1 ? p.a1 + off : nullptr;
-  for (int r = lane; r < n; r += 32) {
-    float o = sq[xpad(r)];
-    if (a1) o = o + a1[r];
-    o = o + (-0.5f) * sa[xpad(r)];
-    dst[r] = o;
+  const bool has_a1 = p.a1 != nullptr;
+#pragma unroll
+  for (int i = 0; i < L; ++i) {
+    const int r = lane + 33 * i;
+    float o = sq[r];
+    if (has_a1) o = o + s1[r];
+    o = o + (-0.5f) * sa[r];
+    dst[lane + 32 * i] = o;
   }
 }
 
@@ -380,6 +416,19 @@ int launch_rhs_k(const RhsArgs& a, dim3 grid, size_t smem, cudaStream_t st) {
     configured = smem;
   }
   kern<<<grid, dim3(LANES, FCHUNKS), smem, st>>>(a);
+  return cuda_status(cudaGetLastError());
+}
+
+template <int L>
+int launch_rhs_x(const RhsXArgs& x, dim3 g, cudaStream_t st) {
+  const size_t sm = (size_t)8 * 3 * xline_pad<L>() * sizeof(float);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(rhs_fast_x<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return cuda_status(e);
+    configured = true;
+  }
+  rhs_fast_x<L><<<g, 256, sm, st>>>(x);
   return cuda_status(cudaGetLastError());
 }
 
@@ -430,12 +479,9 @@ int rhs_axis_fast(Ctx* c, OpPlan* pA, OpPlan* pB, OpPlan* pC, float* out, const 
     fill_warp_op(pC, x.C);
     const dim3 g((unsigned)((a.na + 7) / 8), grid.y);
     const int Lx = n / XCH;
-    const size_t sm = (size_t)8 * 2 * (n + n / 32) * sizeof(float);
-    if (sm > 48 * 1024) return X3D_ERR_UNSUPPORTED;
-    if (Lx == 4) rhs_fast_x<4><<<g, 256, sm, st>>>(x);
-    else if (Lx == 8) rhs_fast_x<8><<<g, 256, sm, st>>>(x);
-    else rhs_fast_x<16><<<g, 256, sm, st>>>(x);
-    return cuda_status(cudaGetLastError());
+    if (Lx == 4) return launch_rhs_x<4>(x, g, st);
+    if (Lx == 8) return launch_rhs_x<8>(x, g, st);
+    return launch_rhs_x<16>(x, g, st);
   }
   const size_t base = (size_t)2 * FCHUNKS * LANES + 2 * LANES;
   const size_t smem = sizeof(float) * (base + (xl ? (size_t)2 * n * LD : (size_t)L * LANES * FCHUNKS));

@@ -125,6 +125,22 @@ class Context:
               "x3d_apply")
         return out
 
+    def conv_diff(self, axis, q, uj, uq, a1=None, nu=1.0, out=None):
+        """One direction's share of the momentum right-hand side of u_q
+        (binary32, fused kernel): nu d_jj u_q + a1 - (d_j(u_j u_q) + u_j d_j u_q) / 2."""
+        torch = _torch()
+        uj = _dev(uj, torch.float32)
+        uq = _dev(uq, torch.float32)
+        if a1 is not None:
+            _dev(a1, torch.float32)
+        if out is None:
+            out = torch.empty_like(uq)
+        dims = (ctypes.c_int * 3)(uq.shape[2], uq.shape[1], uq.shape[0])
+        check(self.lib.x3d_conv_diff_f32(self.h, axis, q, _ptr(out), _ptr(uj), _ptr(uq),
+                                         None if a1 is None else _ptr(a1), ctypes.c_float(nu), dims, _stream()),
+              "x3d_conv_diff_f32")
+        return out
+
     # ---- reference-named routines (FP64) -------------------------------------
     def _colloc(self, fn, t, u, f, s, w, nx, ny, nz, npaire, *pp):
         torch = _torch()

@@ -179,7 +179,7 @@ def dns_dataset(n_dns=512, n_les=128, re=5000.0, dt=0.002, dt_dns=None, t_end=20
             "t": np.array(tdns), "E": np.array(edns), "dns_seconds": secs}
 
 
-def save_dataset(path, d, ntrain=600_000, nval=150_000, seed=0):
+def save_dataset(path, d, ntrain=400_000, nval=100_000, seed=0):
     """A random subsample of the box-filtered data (features, targets) and the
     filtered kinetic-energy history, as an .npz file."""
     torch = _torch()

@@ -70,6 +70,20 @@ def test_host_side_argument_checks(lib):
     assert so.x3d_ctx_create(ctypes.byref(g), ctypes.byref(bad), ctypes.byref(h)) == -7
     assert so.x3d_ctx_create(None, ctypes.byref(o), ctypes.byref(h)) == -1
     assert so.x3d_strerror(-6) == b"coefficient vectors match no set of this context"
+    # fused momentum term: argument, shape and stretching checks come first
+    g = _lib.Grid(16, 16, 16, L, L, L, 0, 0, 0, 0, 0, 0, 0, 0.0)
+    assert so.x3d_ctx_create(ctypes.byref(g), ctypes.byref(o), ctypes.byref(h)) == 0
+    p = ctypes.c_void_p(256)  # never dereferenced
+    one = ctypes.c_float(1.0)
+    assert so.x3d_conv_diff_f32(h, 3, 0, p, p, p, None, one, (ctypes.c_int * 3)(16, 16, 16), None) == -1
+    assert so.x3d_conv_diff_f32(h, 0, 3, p, p, p, None, one, (ctypes.c_int * 3)(16, 16, 16), None) == -1
+    assert so.x3d_conv_diff_f32(h, 0, 0, p, p, p, None, one, (ctypes.c_int * 3)(16, 16, 8), None) == -2
+    so.x3d_ctx_destroy(h)
+    g = _lib.Grid(16, 17, 16, L, L, L, 0, 0, 2, 2, 0, 0, 2, 0.259)
+    assert so.x3d_ctx_create(ctypes.byref(g), ctypes.byref(o), ctypes.byref(h)) == 0
+    assert so.x3d_conv_diff_f32(h, 1, 0, p, p, p, None, one, (ctypes.c_int * 3)(16, 17, 16), None) == -7
+    so.x3d_ctx_destroy(h)
+    assert so.x3d_conv_diff_f32(None, 0, 0, p, p, p, None, one, (ctypes.c_int * 3)(16, 16, 16), None) == -1
     # NULL context handles are rejected before any device work
     assert so.x3d_derx(None, None, None, None, None, None, None, None, 16, 16, 16, 0, 0.0, None) == -1
     assert so.x3d_poisson(None, None, None) == -1
