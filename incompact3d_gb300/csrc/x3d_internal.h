@@ -151,12 +151,14 @@ int mlp_les_tau(Mlp* m, const double* const* g9, double delta, double* const* ta
 
 // Device copies of a plan's vectors (made on first use).
 int upload_plan(OpPlan* p);
-// Fused momentum right-hand side along one axis on the FP32 fast path
-// (x3d_rhs_fast.cu): out = nu*C(uq) + a1 - (A(ua*uq) + ua*B(uq))/2 with A, B
-// first-derivative and C second-derivative plans of that axis; a1 may be null
-// or alias out.  X3D_ERR_UNSUPPORTED when the lines are not fast-path lines.
+// Fused momentum right-hand side along one axis, binary32 periodic lines in
+// circulant form (x3d_conv_diff.cu): out = nu*C(uq) + a1 - (A(ua*uq) + ua*B(uq))/2
+// with A, B first-derivative and C second-derivative plans of that axis; a1
+// may be null or alias out.  X3D_ERR_UNSUPPORTED where no kernel applies
+// (rhs_axis_fast_ok false).
 int rhs_axis_fast(Ctx* c, OpPlan* pA, OpPlan* pB, OpPlan* pC, float* out, const float* ua, const float* uq,
                   const float* a1, float nu, const int* dims, cudaStream_t st);
+bool rhs_axis_fast_ok(const Ctx* c, int axis, const int* dims);
 
 // Get (building on first use) the device plan of an operator.
 int get_plan(Ctx* c, int axis, int kind, int npaire, int coefset, OpPlan** out);

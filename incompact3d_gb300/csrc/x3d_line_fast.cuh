@@ -14,7 +14,7 @@
 //   * the Sherman-Morrison correction is applied only to chunks where the
 //     precomputed vector is non-zero in this precision.
 // The chunk solve is a device function (fast_solve) so that one kernel can
-// run several operators on the same lines (rhs_fast, the momentum right-hand
+// run several operators on the same lines (the momentum right-hand
 // side: three solves per line, one HBM pass per input field).
 #pragma once
 #include "x3d_line_kernel.cuh"

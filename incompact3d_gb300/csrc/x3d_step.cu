@@ -538,11 +538,10 @@ static int momentum_rhs(SolverImpl* s, const T* const* u, T* const* H, cudaStrea
   const T one = T(1), mhalf = T(-0.5), zero = T(0);
   // stretched mesh: dery multiplies by ppy; d2/dy2 gets the pp2y / pp4y terms
   const T* ppy = ymetric<T>(s, 0);
-  if (std::is_same<T, float>::value && !ppy) {
+  if (std::is_same<T, float>::value && !ppy && rhs_axis_fast_ok(c, 1, dims) && rhs_axis_fast_ok(c, 2, dims)) {
     // FP32 periodic lines: one fused kernel per axis runs the three solves of
     // a line (Z, then Y, then X into the history slot)
-    bool fused = true;
-    for (int q = 0; q < 3 && fused; ++q) {
+    for (int q = 0; q < 3; ++q) {
       const int pu[3] = {q == 0 ? 0 : 1, q == 1 ? 0 : 1, q == 2 ? 0 : 1};
       OpPlan* P[3][3];
       for (int ax = 0; ax < 3; ++ax) {
@@ -553,17 +552,10 @@ static int momentum_rhs(SolverImpl* s, const T* const* u, T* const* H, cudaStrea
       float* tzf = (float*)tz;
       const float* uf[3] = {(const float*)u[0], (const float*)u[1], (const float*)u[2]};
       const float* uqf = uf[q];
-      int rc = rhs_axis_fast(c, P[2][0], P[2][1], P[2][2], tzf, uf[2], uqf, nullptr, (float)xnu, dims, st);
-      if (rc == X3D_ERR_UNSUPPORTED && q == 0) {
-        fused = false;
-        break;
-      }
-      RC(rc);
+      RC(rhs_axis_fast(c, P[2][0], P[2][1], P[2][2], tzf, uf[2], uqf, nullptr, (float)xnu, dims, st));
       RC(rhs_axis_fast(c, P[1][0], P[1][1], P[1][2], tzf, uf[1], uqf, tzf, (float)xnu, dims, st));
       s->launches += 2;
-      if (c->grid.nx % 32 == 0 && c->grid.nx / 32 >= 4 && c->grid.nx / 32 <= 16 &&
-          (c->grid.nx / 32 & (c->grid.nx / 32 - 1)) == 0) {
-        // x lines: one warp per line (no tile)
+      if (rhs_axis_fast_ok(c, 0, dims)) {
         RC(rhs_axis_fast(c, P[0][0], P[0][1], P[0][2], (float*)H[q], uf[0], uqf, tzf, (float)xnu, dims, st));
         s->launches++;
       } else {
@@ -575,7 +567,7 @@ static int momentum_rhs(SolverImpl* s, const T* const* u, T* const* H, cudaStrea
         RC(op<T>(s, 0, K_DER2, pu[0], H[q], u[q], dims, st, &f));
       }
     }
-    if (fused) return cuda_status(cudaGetLastError());
+    return cuda_status(cudaGetLastError());
   }
   for (int q = 0; q < 3; ++q) {
     const T* uq = u[q];
