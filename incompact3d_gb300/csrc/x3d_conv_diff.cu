@@ -7,7 +7,9 @@
 // compact solves of a line back to back:
 //   out = (nu C(u_q) + a1) - (A(u_j u_q) + u_j B(u_q)) / 2
 // so u_j, u_q and the running sum a1 are read from HBM once and out is written
-// once (4 field passes instead of 11 with one kernel per solve).
+// once (4 field passes instead of 11 with one kernel per solve).  The x kernel
+// rounds in that order; the y/z kernel accumulates a1 + (nu C - A/2 - u_j B/2)
+// (same terms, binary32 round-off apart).
 //
 // Periodic solves in circulant form.  On a periodic line the compact matrix
 // of every operator here is circulant, A = I + alpha (S + S^-1) with S the
@@ -25,6 +27,7 @@
 // ((-mu)^(jL) < 2^-32) are dropped, which is exact to round-off for the
 // chunk lengths used (L >= 4, |mu| <= 0.39).
 #include <cmath>
+#include <cstdint>
 
 #include "x3d_line_fast.cuh"
 
@@ -84,33 +87,6 @@ __device__ __forceinline__ void circ_warp(const float* w, float* v, const CircOp
   for (int k = 0; k < L; ++k) v[k] = fmaf(p.qw[k], cb, v[k]);
 }
 
-// Block solve: thread (lane, ch) owns rows ch*L .. ch*L+L-1 of line `lane`;
-// FC chunks per line, carries through shared memory (ef / eb: [FC][32]).
-// Two block barriers; every thread of the block must call it.
-template <int KIND, int L, int FC>
-__device__ __forceinline__ void circ_block(const float* w, float* v, const CircOp& p, float* ef, float* eb, int ch,
-                                           int lane) {
-  constexpr int LO = Halo<KIND>::lo;
-#pragma unroll
-  for (int k = 0; k < L; ++k) v[k] = circ_rhs<KIND, LO>(w, k, p);
-#pragma unroll
-  for (int k = 1; k < L; ++k) v[k] = fmaf(p.nmu, v[k - 1], v[k]);
-  ef[ch * 32 + lane] = v[L - 1];
-  __syncthreads();
-  float c = 0.f;
-  for (int j = p.J; j >= 1; --j) c = fmaf(p.Ach, c, ef[((ch - j) & (FC - 1)) * 32 + lane]);
-#pragma unroll
-  for (int k = 0; k < L; ++k) v[k] = fmaf(p.pw[k], c, v[k]);
-#pragma unroll
-  for (int k = L - 2; k >= 0; --k) v[k] = fmaf(p.nmu, v[k + 1], v[k]);
-  eb[ch * 32 + lane] = v[0];
-  __syncthreads();
-  c = 0.f;
-  for (int j = p.J; j >= 1; --j) c = fmaf(p.Ach, c, eb[((ch + j) & (FC - 1)) * 32 + lane]);
-#pragma unroll
-  for (int k = 0; k < L; ++k) v[k] = fmaf(p.qw[k], c, v[k]);
-}
-
 // Asynchronous 4-byte global -> shared copy (LDGSTS): the copies are in
 // flight together and hold no registers.
 __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
@@ -136,7 +112,8 @@ struct CdArgs {
 // ---- x lines: one warp per line -------------------------------------------
 // The line is contiguous: a warp stages it (u_q, u_j with a 4-row periodic
 // halo at each end, and a1) into its own padded shared buffers with cp.async,
-// then lane t solves rows t*L .. t*L+L-1 from there.  Row r lives at
+// then lane t solves rows t*L .. t*L+L-1 from there and stores its L
+// contiguous results with 16-byte stores.  Row r lives at
 //   P(r + L),  P(s) = s + floor(s / L),
 // so the window of lane t is (L+1)(t+1) + d + floor(d/L) for row t*L + d:
 // compile-time offsets from one base, and a stride of L+1 (odd) across the
@@ -150,12 +127,16 @@ __device__ __forceinline__ constexpr int hoff(int d) {
   return d + (d >= 0 ? d / L : -1);  // -L <= d < 2L
 }
 
+// Warps (lines) per block and blocks per SM: 4 x 5 = 20 warps, ~100 registers
+// per thread for the three solves of L = 16 rows without spills.
+constexpr int XW = 4, XB = 5;
+
 template <int L>
-__global__ void __launch_bounds__(256, 3) conv_diff_x(const __grid_constant__ CdArgs p) {
+__global__ void __launch_bounds__(32 * XW, XB) conv_diff_x(const __grid_constant__ CdArgs p) {
   extern __shared__ __align__(16) float smx[];
   constexpr int N = 32 * L, NB = xbuf<L>(), STEP = 32 + 32 / L;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int line = blockIdx.x * 8 + warp;
+  const int line = blockIdx.x * XW + warp;
   if (line >= p.na) return;  // whole warps only: the shuffles stay converged
   float* sq = smx + (size_t)warp * 3 * NB;
   float* sa = sq + NB;
@@ -188,149 +169,199 @@ __global__ void __launch_bounds__(256, 3) conv_diff_x(const __grid_constant__ Cd
   __syncwarp();
   const float* bq = sq + (L + 1) * (lane + 1);
   const float* ba = sa + (L + 1) * (lane + 1);
-  float vB[L], v[L];
+  float conv[L], v[L];
   {
-    float wq[L + 8];  // u_q rows -4 .. L+3 of this lane's chunk
-#pragma unroll
-    for (int j = 0; j < L + 8; ++j) wq[j] = bq[hoff<L>(j - 4)];
-    circ_warp<K_DER1, L>(wq + 2, vB, p.B, lane);
-    circ_warp<K_DER2, L>(wq, v, p.C, lane);
-  }
-  cp_async_wait<0>();
-  __syncwarp();
-  float* b1 = s1 + (L + 1) * (lane + 1);
-  if (p.a1) {
-#pragma unroll
-    for (int k = 0; k < L; ++k) b1[k] = __fadd_rn(__fmul_rn(p.nu, v[k]), b1[k]);
-  } else {
-#pragma unroll
-    for (int k = 0; k < L; ++k) b1[k] = __fmul_rn(p.nu, v[k]);
-  }
-  {
-    float w[L + 4];  // (u_j u_q) rows -2 .. L+1
+    float w[L + 4];  // A: d_j(u_j u_q), rows -2 .. L+1
 #pragma unroll
     for (int j = 0; j < L + 4; ++j) w[j] = bq[hoff<L>(j - 2)] * ba[hoff<L>(j - 2)];
-    circ_warp<K_DER1, L>(w, v, p.A, lane);
+    circ_warp<K_DER1, L>(w, conv, p.A, lane);
   }
+  float wq[L + 8];  // u_q rows -4 .. L+3 of this lane's chunk (B and C)
 #pragma unroll
-  for (int k = 0; k < L; ++k) v[k] = fmaf(ba[k], vB[k], v[k]);  // conv = A + u_j B
-  __syncwarp();  // every lane has read its windows of sq / sa
-  float* bo = sa + (L + 1) * (lane + 1);
+  for (int j = 0; j < L + 8; ++j) wq[j] = bq[hoff<L>(j - 4)];
+  circ_warp<K_DER1, L>(wq + 2, v, p.B, lane);
 #pragma unroll
-  for (int k = 0; k < L; ++k) bo[k] = v[k];
+  for (int k = 0; k < L; ++k) conv[k] = fmaf(ba[k], v[k], conv[k]);  // A + u_j B
+  circ_warp<K_DER2, L>(wq, v, p.C, lane);
+  cp_async_wait<0>();
   __syncwarp();
-  float* dst = p.out + off;
+  // out = (nu C + a1) - conv / 2 for this lane's L contiguous rows (16-byte stores)
+  const float* b1 = s1 + (L + 1) * (lane + 1);
+  float4* dst = reinterpret_cast<float4*>(p.out + off + L * lane);
 #pragma unroll
-  for (int i = 0; i < L; ++i) {
-    const int s = st0 + i * STEP;
-    dst[lane + 32 * i] = fmaf(-0.5f, sa[s], s1[s]);
-  }
-}
-
-// ---- y / z lines: one thread per line across x, FC chunks per line --------
-// Block (32 lanes, FC chunks): lane = line (32 consecutive x: one coalesced
-// 128-byte segment per row), chunk ch = rows ch*L .. ch*L+L-1 of the line.
-// Windows come straight from HBM / L2 into registers (u_q is read once per
-// solve: the second and third reads hit L1 / L2); a1 is prefetched into
-// shared memory with cp.async at the start; B(u_q) waits in shared memory
-// while C and A are solved.
-template <int WN, int N>
-__device__ __forceinline__ void yz_window(float* w, const float* src, int r0m, int rs, bool edge) {
-  if (edge) {
+  for (int k4 = 0; k4 < L / 4; ++k4) {
+    float o[4];
 #pragma unroll
-    for (int j = 0; j < WN; ++j) {
-      int r = r0m + j;
-      r = (r < 0) ? r + N : ((r >= N) ? r - N : r);
-      w[j] = src[r * rs];
+    for (int m = 0; m < 4; ++m) {
+      const int k = 4 * k4 + m;
+      float c = __fmul_rn(p.nu, v[k]);
+      if (p.a1) c = __fadd_rn(c, b1[k]);
+      o[m] = fmaf(-0.5f, conv[k], c);
     }
-  } else {
-    const float* s = src + r0m * rs;
-#pragma unroll
-    for (int j = 0; j < WN; ++j) w[j] = s[j * rs];
+    dst[k4] = make_float4(o[0], o[1], o[2], o[3]);
   }
 }
 
-template <int WN, int N>
-__device__ __forceinline__ void yz_window_prod(float* w, const float* src, const float* src2, int r0m, int rs,
-                                               bool edge) {
-  if (edge) {
-#pragma unroll
-    for (int j = 0; j < WN; ++j) {
-      int r = r0m + j;
-      r = (r < 0) ? r + N : ((r >= N) ? r - N : r);
-      w[j] = src[r * rs] * src2[r * rs];
+// ---- y / z lines: two lines per thread, FC chunks per line -----------------
+// Block: 8 column pairs (16 consecutive x lines) x FC chunks of L = 8 rows.
+// The block first copies its slab of u_q and u_j (all N rows of its 16 lines
+// plus 4 periodic halo rows at each end) into shared memory with 8-byte
+// cp.async: every HBM load of the block is in flight at once, and two blocks
+// per SM overlap one's copy with the other's solves.  A thread then reads its
+// two lines as float2 (half the shared-memory instructions of one line per
+// thread, and two independent recurrence chains).  The three results are
+// accumulated in registers as r = nu C - A/2 - u_j B/2 (the solves in the
+// order C, A, B) and out = a1 + r is written with a1 read in the epilogue.
+// Slab row r (-4 <= r < N+4), line c sits at (r + 4) * 18 + c: the chunks of a
+// half-warp (rows 8 apart: 8 * 18 = 16 mod 32 words) fall in disjoint banks.
+constexpr int YL = 8;     // rows per chunk
+constexpr int CP = 8;     // column pairs per block
+constexpr int SR2 = 18;   // slab row stride (floats)
+
+__device__ __forceinline__ float2 f2fma(float a, float2 b, float2 c) {
+  return make_float2(fmaf(a, b.x, c.x), fmaf(a, b.y, c.y));
+}
+__device__ __forceinline__ float2 f2fma2(float2 a, float2 b, float2 c) {
+  return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+}
+
+template <int KIND, int LO>
+__device__ __forceinline__ float2 circ_rhs2(const float2* w, int k, const CircOp& p) {
+#define W_(d) w[k + LO + (d)]
+  if constexpr (KIND == K_DER1) {
+    return make_float2(p.c1 * (W_(1).x - W_(-1).x) + p.c2 * (W_(2).x - W_(-2).x),
+                       p.c1 * (W_(1).y - W_(-1).y) + p.c2 * (W_(2).y - W_(-2).y));
+  } else {
+    const float2 ur = W_(0);
+    float ax = p.c1 * (W_(1).x - ur.x - ur.x + W_(-1).x) + p.c2 * (W_(2).x - ur.x - ur.x + W_(-2).x);
+    float ay = p.c1 * (W_(1).y - ur.y - ur.y + W_(-1).y) + p.c2 * (W_(2).y - ur.y - ur.y + W_(-2).y);
+    if (p.nterms > 2) {
+      ax = ax + p.c3 * (W_(3).x - ur.x - ur.x + W_(-3).x) + p.c4 * (W_(4).x - ur.x - ur.x + W_(-4).x);
+      ay = ay + p.c3 * (W_(3).y - ur.y - ur.y + W_(-3).y) + p.c4 * (W_(4).y - ur.y - ur.y + W_(-4).y);
     }
-  } else {
-    const float* s = src + r0m * rs;
-    const float* s2 = src2 + r0m * rs;
-#pragma unroll
-    for (int j = 0; j < WN; ++j) w[j] = s[j * rs] * s2[j * rs];
+    return make_float2(ax, ay);
   }
+#undef W_
 }
 
-template <int L, int FC>
+// Block solve of two lines per thread: thread (cp, ch) owns rows ch*L ..
+// ch*L+L-1 of lines 2cp and 2cp+1; FC chunks per line, carries through shared
+// memory (ef / eb: [FC][CP] float2).  Two block barriers; every thread of the
+// block must call it.
+template <int KIND, int L, int FC>
+__device__ __forceinline__ void circ_block2(const float2* w, float2* v, const CircOp& p, float2* ef, float2* eb,
+                                            int ch, int cp) {
+  constexpr int LO = Halo<KIND>::lo;
+#pragma unroll
+  for (int k = 0; k < L; ++k) v[k] = circ_rhs2<KIND, LO>(w, k, p);
+#pragma unroll
+  for (int k = 1; k < L; ++k) v[k] = f2fma(p.nmu, v[k - 1], v[k]);
+  ef[ch * CP + cp] = v[L - 1];
+  __syncthreads();
+  float2 c = make_float2(0.f, 0.f);
+  for (int j = p.J; j >= 1; --j) c = f2fma(p.Ach, c, ef[((ch - j) & (FC - 1)) * CP + cp]);
+#pragma unroll
+  for (int k = 0; k < L; ++k) v[k] = f2fma2(make_float2(p.pw[k], p.pw[k]), c, v[k]);
+#pragma unroll
+  for (int k = L - 2; k >= 0; --k) v[k] = f2fma(p.nmu, v[k + 1], v[k]);
+  eb[ch * CP + cp] = v[0];
+  __syncthreads();
+  c = make_float2(0.f, 0.f);
+  for (int j = p.J; j >= 1; --j) c = f2fma(p.Ach, c, eb[((ch + j) & (FC - 1)) * CP + cp]);
+#pragma unroll
+  for (int k = 0; k < L; ++k) v[k] = f2fma2(make_float2(p.qw[k], p.qw[k]), c, v[k]);
+}
+
+__device__ __forceinline__ void cp_async8(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+template <int FC>
 __host__ __device__ constexpr size_t yz_smem() {
-  return sizeof(float) * ((size_t)2 * L * 32 * FC + 2 * 32 * FC);
+  return sizeof(float) * ((size_t)2 * (YL * FC + 8) * SR2 + (size_t)4 * FC * CP);
 }
 
-template <int L, int FC>
-__global__ void __launch_bounds__(32 * FC, (FC >= 32) ? 1 : 2) conv_diff_yz(const __grid_constant__ CdArgs p) {
+template <int FC>
+__global__ void __launch_bounds__(CP* FC, (CP * FC <= 512) ? 2 : 1) conv_diff_yz(const __grid_constant__ CdArgs p) {
   extern __shared__ __align__(16) float smy[];
-  constexpr int N = L * FC, NT = 32 * FC;
-  float* stash = smy;           // [L][NT]: B(u_q)
-  float* s1 = stash + L * NT;   // [L][NT]: a1, then nu C + a1
-  float* ef = s1 + L * NT;      // [FC][32]
-  float* eb = ef + 32 * FC;     // [FC][32]
-  const int lane = threadIdx.x, ch = threadIdx.y, tid = ch * 32 + lane;
-  const int a0 = blockIdx.x * 32;
-  const bool ok = a0 + lane < p.na;
-  // lanes past the last line solve line a0 (valid memory) and store nothing
-  const long long base = (long long)(ok ? a0 + lane : a0) * p.sa + (long long)blockIdx.y * p.sb;
-  const int rs = p.rs, r0 = ch * L;
-  const bool edge = (ch == 0 || ch == FC - 1);
-  const float* q = p.uq + base;
-  const float* ua = p.ua + base;
-  if (p.a1) {
-    const float* g1 = p.a1 + base + (long long)r0 * rs;
-#pragma unroll
-    for (int k = 0; k < L; ++k) cp_async4(s1 + k * NT + tid, g1 + k * rs);
-  }
-  cp_async_commit();
-  float v[L];
+  constexpr int L = YL, N = L * FC, NT = CP * FC, SLAB = (N + 8) * SR2;
+  float* su = smy;
+  float* sa = su + SLAB;
+  float2* ef = reinterpret_cast<float2*>(sa + SLAB);
+  float2* eb = ef + FC * CP;
+  const int cp = threadIdx.x, ch = threadIdx.y, t = ch * CP + cp;
+  const long long pb = (long long)blockIdx.y * p.sb + (long long)blockIdx.x * 2 * CP;
+  const int rs = p.rs;
   {
-    float wq[L + 4];  // u_q rows r0-2 .. r0+L+1
-    yz_window<L + 4, N>(wq, q, r0 - 2, rs, edge);
-    circ_block<K_DER1, L, FC>(wq, v, p.B, ef, eb, ch, lane);
-  }
+    // float2 element e = t + NT i -> row e / 8, pair e % 8 (a warp copies four
+    // 64-byte row segments per instruction)
 #pragma unroll
-  for (int k = 0; k < L; ++k) stash[k * NT + tid] = v[k];
-  {
-    float wq[L + 8];  // u_q rows r0-4 .. r0+L+3 (again: L1 / L2 hits)
-    yz_window<L + 8, N>(wq, q, r0 - 4, rs, edge);
-    circ_block<K_DER2, L, FC>(wq, v, p.C, ef, eb, ch, lane);
-  }
-  cp_async_wait<0>();  // own entries only: no barrier needed
-  if (p.a1) {
-#pragma unroll
-    for (int k = 0; k < L; ++k) s1[k * NT + tid] = __fadd_rn(__fmul_rn(p.nu, v[k]), s1[k * NT + tid]);
-  } else {
-#pragma unroll
-    for (int k = 0; k < L; ++k) s1[k * NT + tid] = __fmul_rn(p.nu, v[k]);
-  }
-  {
-    float w[L + 4];  // (u_j u_q) rows r0-2 .. r0+L+1
-    yz_window_prod<L + 4, N>(w, q, ua, r0 - 2, rs, edge);
-    circ_block<K_DER1, L, FC>(w, v, p.A, ef, eb, ch, lane);
-  }
-  if (ok) {
-    const float* uj = ua + (long long)r0 * rs;
-    float* dst = p.out + base + (long long)r0 * rs;
-#pragma unroll
-    for (int k = 0; k < L; ++k) {
-      const float conv = fmaf(uj[k * rs], stash[k * NT + tid], v[k]);  // A + u_j B
-      dst[k * rs] = fmaf(-0.5f, conv, s1[k * NT + tid]);
+    for (int i = 0; i < L; ++i) {
+      const int e = t + NT * i;
+      const int r = e >> 3, c = 2 * (e & 7);
+      const long long g = pb + (long long)r * rs + c;
+      const int d = (r + 4) * SR2 + c;
+      cp_async8(su + d, p.uq + g);
+      cp_async8(sa + d, p.ua + g);
     }
+    if (t < 8 * CP) {  // halo rows -4..-1 <- N-4..N-1 and N..N+3 <- 0..3
+      const int h = t >> 3, c = 2 * (t & 7);
+      const int r = (h < 4) ? h - 4 : N + h - 4;
+      const int rg = (h < 4) ? N - 4 + h : h - 4;
+      const long long g = pb + (long long)rg * rs + c;
+      const int d = (r + 4) * SR2 + c;
+      cp_async8(su + d, p.uq + g);
+      cp_async8(sa + d, p.ua + g);
+    }
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
   }
+  constexpr int R2 = SR2 / 2;  // slab row stride in float2
+  const int o0 = ((ch * L + 4) * SR2 + 2 * cp) / 2;
+  const float2* bu = reinterpret_cast<const float2*>(su) + o0;
+  const float2* ba = reinterpret_cast<const float2*>(sa) + o0;
+  float2 v[L], r[L];
+  {
+    float2 w[L + 8];  // C: d_jj u_q, rows r0-4 .. r0+L+3
+#pragma unroll
+    for (int j = 0; j < L + 8; ++j) w[j] = bu[(j - 4) * R2];
+    circ_block2<K_DER2, L, FC>(w, v, p.C, ef, eb, ch, cp);
+  }
+#pragma unroll
+  for (int k = 0; k < L; ++k) r[k] = make_float2(p.nu * v[k].x, p.nu * v[k].y);
+  {
+    float2 w[L + 4];  // A: d_j(u_j u_q), rows r0-2 .. r0+L+1
+#pragma unroll
+    for (int j = 0; j < L + 4; ++j) {
+      const float2 q = bu[(j - 2) * R2], a = ba[(j - 2) * R2];
+      w[j] = make_float2(q.x * a.x, q.y * a.y);
+    }
+    circ_block2<K_DER1, L, FC>(w, v, p.A, ef, eb, ch, cp);
+  }
+#pragma unroll
+  for (int k = 0; k < L; ++k) r[k] = f2fma(-0.5f, v[k], r[k]);
+  {
+    float2 w[L + 4];  // B: d_j u_q
+#pragma unroll
+    for (int j = 0; j < L + 4; ++j) w[j] = bu[(j - 2) * R2];
+    circ_block2<K_DER1, L, FC>(w, v, p.B, ef, eb, ch, cp);
+  }
+#pragma unroll
+  for (int k = 0; k < L; ++k) {
+    const float2 uj = ba[k * R2];
+    r[k] = f2fma2(make_float2(-0.5f * uj.x, -0.5f * uj.y), v[k], r[k]);
+  }
+  // a1 may alias out: this thread reads its own rows of a1 before writing them
+  const long long o = pb + 2 * cp + (long long)(ch * L) * rs;
+  float2 a1v[L];
+#pragma unroll
+  for (int k = 0; k < L; ++k)
+    a1v[k] = p.a1 ? *reinterpret_cast<const float2*>(p.a1 + o + (long long)k * rs) : make_float2(0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < L; ++k)
+    *reinterpret_cast<float2*>(p.out + o + (long long)k * rs) = make_float2(a1v[k].x + r[k].x, a1v[k].y + r[k].y);
 }
 
 // ---- host side -------------------------------------------------------------
@@ -370,27 +401,27 @@ static int fill_circ(const OpPlan* p, int L, int max_carries, CircOp& c) {
 
 template <int L>
 static int launch_cd_x(const CdArgs& a, dim3 g, cudaStream_t st) {
-  const size_t sm = (size_t)8 * 3 * xbuf<L>() * sizeof(float);
+  const size_t sm = (size_t)XW * 3 * xbuf<L>() * sizeof(float);
   static bool configured = false;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(conv_diff_x<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return cuda_status(e);
     configured = true;
   }
-  conv_diff_x<L><<<g, 256, sm, st>>>(a);
+  conv_diff_x<L><<<g, 32 * XW, sm, st>>>(a);
   return cuda_status(cudaGetLastError());
 }
 
-template <int L, int FC>
+template <int FC>
 static int launch_cd_yz(const CdArgs& a, dim3 g, cudaStream_t st) {
-  constexpr size_t sm = yz_smem<L, FC>();
+  constexpr size_t sm = yz_smem<FC>();
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(conv_diff_yz<L, FC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(conv_diff_yz<FC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return cuda_status(e);
     configured = true;
   }
-  conv_diff_yz<L, FC><<<g, dim3(32, FC), sm, st>>>(a);
+  conv_diff_yz<FC><<<g, dim3(CP, FC), sm, st>>>(a);
   return cuda_status(cudaGetLastError());
 }
 
@@ -403,10 +434,10 @@ static bool cd_shape(int axis, int n, int* L, int* FC) {
     *FC = 32;
     return true;
   }
-  if (n == 128) { *L = 8; *FC = 16; return true; }
-  if (n == 256) { *L = 16; *FC = 16; return true; }
-  if (n == 512) { *L = 16; *FC = 32; return true; }
-  return false;
+  if (n != 128 && n != 256 && n != 512) return false;
+  *L = YL;
+  *FC = n / YL;
+  return true;
 }
 
 }  // namespace lk
@@ -418,6 +449,7 @@ bool rhs_axis_fast_ok(const Ctx* c, int axis, const int* dims) {
   if (!c->fast_lines || !c->ax[axis].periodic || !cd_shape(axis, dims[axis], &L, &FC)) return false;
   if (axis == 1 && c->st.istret != 0) return false;
   const long long rs = (axis == 0) ? 1 : (axis == 1 ? (long long)dims[0] : (long long)dims[0] * dims[1]);
+  if (axis != 0 && dims[0] % (2 * CP) != 0) return false;  // y/z blocks: 16 whole x lines
   return (long long)dims[axis] * rs < (1LL << 31);
 }
 
@@ -444,28 +476,35 @@ int rhs_axis_fast(Ctx* c, OpPlan* pA, OpPlan* pB, OpPlan* pC, float* out, const 
   if (rc != X3D_OK) return rc;
   const long long nx = dims[0], ny = dims[1], nz = dims[2];
   if (axis == 0) {
-    // warp per x line: lines (j, k) with j in a block of 8, k = blockIdx.y
+    // warp per x line: lines (j, k) with j in a block of XW, k = blockIdx.y;
+    // each lane stores its L rows as float4
+    // each lane stores its L rows as float4
+    if (reinterpret_cast<uintptr_t>(out) % 16 != 0) return X3D_ERR_UNSUPPORTED;
     a.na = (int)ny;
     a.sa = nx;
     a.sb = nx * ny;
     a.rs = 1;
     if (nz > 65535) return X3D_ERR_UNSUPPORTED;
-    const dim3 g((unsigned)((ny + 7) / 8), (unsigned)nz);
+    const dim3 g((unsigned)((ny + XW - 1) / XW), (unsigned)nz);
     if (L == 4) return launch_cd_x<4>(a, g, st);
     if (L == 8) return launch_cd_x<8>(a, g, st);
     return launch_cd_x<16>(a, g, st);
   }
-  // y lines: (i, k), z lines: (i, j); 32 consecutive i per block
+  // y lines: (i, k), z lines: (i, j); 16 consecutive i per block
   a.na = (int)nx;
   a.sa = 1;
   a.sb = (axis == 1) ? nx * ny : nx;
   a.rs = (int)((axis == 1) ? nx : nx * ny);
   const long long planes = (axis == 1) ? nz : ny;
   if (planes > 65535) return X3D_ERR_UNSUPPORTED;
-  const dim3 g((unsigned)((nx + 31) / 32), (unsigned)planes);
-  if (L == 8) return launch_cd_yz<8, 16>(a, g, st);
-  if (FC == 16) return launch_cd_yz<16, 16>(a, g, st);
-  return launch_cd_yz<16, 32>(a, g, st);
+  // 8-byte copies and stores of line pairs
+  if ((reinterpret_cast<uintptr_t>(out) | reinterpret_cast<uintptr_t>(ua) | reinterpret_cast<uintptr_t>(uq) |
+       reinterpret_cast<uintptr_t>(a1)) % 8 != 0)
+    return X3D_ERR_UNSUPPORTED;
+  const dim3 g((unsigned)(nx / (2 * CP)), (unsigned)planes);
+  if (FC == 16) return launch_cd_yz<16>(a, g, st);
+  if (FC == 32) return launch_cd_yz<32>(a, g, st);
+  return launch_cd_yz<64>(a, g, st);
 }
 
 }  // namespace x3d
