@@ -33,10 +33,11 @@ METRIC = "TGV 512^3 Mpts*steps/s (mixed FP32/FP64 step; FP64 step reported besid
 UNIT = "Mpts*steps/s"
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one y-line FP32 first
-# derivative launch on the 512^3 field (ncu --set full capture of
-# `bench.py --workload ops --n 512 --ops dery --dtypes f32 --bcs 0 --reps 1`)
-DERY_F32_512_DRAM_BYTES = 1025895680
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the fused
+# y-line momentum kernel (conv_diff_yz, reads u_j, u_q, a1 and writes out) on
+# the 512^3 FP32 fields (ncu --set full capture of
+# `bench.py --workload ops --n 512 --ops convdiffy --reps 1`)
+CONVDIFF_Y_F32_512_DRAM_BYTES = 1610714112 + 515571200
 
 
 def dist_env():
@@ -242,12 +243,16 @@ def run_ours(args):
     e2e = {"value": round(N / e2e_secs / 1e6 * ws, 3), "unit": UNIT, "h2d_bytes_per_step": 3 * N * 8,
            "d2h_bytes_per_step": 3 * N * 8}
     del host
-    # dominant kernel, timed alone with CUDA events: y-direction compact first
-    # derivative in FP32 on the 512^3 field (algorithmic bytes = (N_in+N_out)*4)
-    u32 = torch.randn((n, n, n), dtype=torch.float32, device="cuda")
-    o32 = torch.empty_like(u32)
-    ksec = time_kernel(torch, lambda: ctx.apply(1, x3d.OP_DER1, 0, u32, out=o32), 20, stream)
-    kbytes = 2 * N * 4
+    # dominant kernel by launch-list share, timed alone with CUDA events: the
+    # fused y-line momentum kernel on 512^3 FP32 fields (algorithmic bytes:
+    # read u_j, u_q, a1, write out = 4 N * 4)
+    uj32 = torch.randn((n, n, n), dtype=torch.float32, device="cuda")
+    uq32 = torch.randn((n, n, n), dtype=torch.float32, device="cuda")
+    a132 = torch.randn((n, n, n), dtype=torch.float32, device="cuda")
+    o32 = torch.empty_like(uq32)
+    ksec = time_kernel(torch, lambda: ctx.conv_diff(1, 0, uj32, uq32, a132, 1 / 1600.0, out=o32), 20, stream)
+    kbytes = 4 * N * 4
+    del uj32, uq32, a132, o32
     u64 = torch.randn((n, n, n), dtype=torch.float64, device="cuda")
     o64 = torch.empty_like(u64)
     ksec64 = time_kernel(torch, lambda: ctx.apply(1, x3d.OP_DER1, 0, u64, out=o64), 10, stream)
@@ -272,8 +277,8 @@ def run_ours(args):
         "gpu_launches": int(main["launches"] * args.steps),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk, "unit": "GB/s",
                      "frac": round(achieved / pk, 4),
-                     "traffic": DERY_F32_512_DRAM_BYTES if n == 512 else None,
-                     "kernel": "line_kernel<float,DER1> y-lines 512^3 (dery FP32)",
+                     "traffic": CONVDIFF_Y_F32_512_DRAM_BYTES if n == 512 else None,
+                     "kernel": "conv_diff_yz (fused y-line momentum RHS, 3 compact solves, FP32) 512^3",
                      "peak_source": pk_kind},
         "cpu_baseline": {"value": round(cpu_rate, 4) if cpu_rate else None, "unit": UNIT, "cores": cpu_threads,
                          "kind": "port",
