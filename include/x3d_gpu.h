@@ -281,6 +281,13 @@ int x3d_transpose_y_to_x(x3d_ctx* ctx, const double* src, double* dst, long long
 int x3d_divergence(x3d_ctx* ctx, double* pp3, const double* ux, const double* uy, const double* uz,
                    void* stream);
 int x3d_gradp(x3d_ctx* ctx, double* px, double* py, double* pz, const double* pp3, void* stream);
+/* binary32 builds of divergence (FP64 result, as the mixed-precision step
+ * hands it to the Poisson solve) and gradp, same staggered-operator sequence;
+ * on periodic lines of 128, 256 or 512 points they run the circulant-form
+ * kernels with the y / z sums and pairs fused.  Uniform meshes only
+ * (X3D_ERR_UNSUPPORTED for istret != 0). */
+int x3d_divergence_f32(x3d_ctx* ctx, double* pp3, const float* ux, const float* uy, const float* uz, void* stream);
+int x3d_gradp_f32(x3d_ctx* ctx, float* px, float* py, float* pz, const float* pp3, void* stream);
 int x3d_cor_vel(x3d_ctx* ctx, double* ux, double* uy, double* uz, const double* px, const double* py,
                 const double* pz, void* stream);
 

@@ -110,6 +110,8 @@ def load():
             getattr(lib, "x3d_transpose_" + n).argtypes = [P, P, P, LL, P]
         lib.x3d_divergence.argtypes = [P, P, P, P, P, P]
         lib.x3d_gradp.argtypes = [P, P, P, P, P, P]
+        lib.x3d_divergence_f32.argtypes = [P, P, P, P, P, P]
+        lib.x3d_gradp_f32.argtypes = [P, P, P, P, P, P]
         lib.x3d_cor_vel.argtypes = [P, P, P, P, P, P, P, P]
         lib.x3d_solver_create.argtypes = [P, ctypes.POINTER(SolverOpts), ctypes.POINTER(P)]
         lib.x3d_solver_destroy.argtypes = [P]

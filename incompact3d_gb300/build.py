@@ -33,9 +33,12 @@ def up_to_date():
     return all(os.path.getmtime(p) <= t for p in _deps())
 
 
+# Host code (the coefficient tables, stretching metrics, plans) is compiled
+# without FMA contraction so it rounds as the reference's formulas do on
+# every host (aarch64 compilers contract a*b+c by default).
 def _compile(src, extra):
     obj = os.path.join(OUTDIR, os.path.basename(src) + ".o")
-    cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+    cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
            "-I", os.path.join(ROOT, "include"), "-I", CSRC, *extra, "-c", src, "-o", obj]
     if src.endswith(".cpp"):
         cmd = [NVCC, "-x", "cu", *cmd[1:]]

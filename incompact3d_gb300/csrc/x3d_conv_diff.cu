@@ -9,95 +9,15 @@
 // so u_j, u_q and the running sum a1 are read from HBM once and out is written
 // once (4 field passes instead of 11 with one kernel per solve).  The x kernel
 // rounds in that order; the y/z kernel accumulates a1 + (nu C - A/2 - u_j B/2)
-// (same terms, binary32 round-off apart).
-//
-// Periodic solves in circulant form.  On a periodic line the compact matrix
-// of every operator here is circulant, A = I + alpha (S + S^-1) with S the
-// cyclic shift, and factors exactly as
-//   A = (I + mu S)(I + mu S^-1) / (1 + mu^2),  mu = 2 alpha / (1 + sqrt(1 - 4 alpha^2)),
-// so x = A^-1 b is a forward recurrence z_i = (1 + mu^2) b_i - mu z_{i-1}
-// followed by a backward one x_i = z_i - mu x_{i+1}, both cyclic.  The reference
-// solves the same system by Thomas sweeps of a corner-modified matrix plus a
-// Sherman-Morrison correction (src/derive.f90:7-64); both give A^-1 b, to
-// round-off.  In this form every row has the same coefficients, so a chunk of
-// L rows is solved locally from a zero carry and corrected by
-//   z_k += (-mu)^(k+1) c_in,      x_k += (-mu)^(L-k) c_in',
-// where the carries c_in come from a cyclic scan of the chunk ends with the
-// constant multiplier (-mu)^L; terms below binary32 resolution
-// ((-mu)^(jL) < 2^-32) are dropped, which is exact to round-off for the
-// chunk lengths used (L >= 4, |mu| <= 0.39).
+// (same terms, binary32 round-off apart).  The solves are in circulant form
+// (x3d_circ.cuh).
 #include <cmath>
 #include <cstdint>
 
-#include "x3d_line_fast.cuh"
+#include "x3d_circ.cuh"
 
 namespace x3d {
 namespace lk {
-
-// One periodic compact operator in circulant form (binary32).
-struct CircOp {
-  float c1, c2, c3, c4;  // interior stencil coefficients times (1 + mu^2)
-  float nmu;             // -mu
-  int nterms;            // second derivative: 2 or 4 stencil terms
-  int J;                 // chunk carries that reach binary32 (block kernel)
-  float Ach;             // (-mu)^L: carry multiplier across one chunk
-  float ak[5];           // Ach^(2^s): cyclic warp scan, s = 0..4
-  float pw[32];          // (-mu)^(k+1): forward fix-up of chunk row k
-  float qw[32];          // (-mu)^(L-k): backward fix-up of chunk row k
-};
-
-// Interior stencil (right-hand side B u) on the window w, w[j] = u[r0 - LO + j].
-template <int KIND, int LO>
-__device__ __forceinline__ float circ_rhs(const float* w, int k, const CircOp& p) {
-#define W_(d) w[k + LO + (d)]
-  if constexpr (KIND == K_DER1) {
-    return p.c1 * (W_(1) - W_(-1)) + p.c2 * (W_(2) - W_(-2));
-  } else {
-    const float ur = W_(0);
-    float acc = p.c1 * (W_(1) - ur - ur + W_(-1)) + p.c2 * (W_(2) - ur - ur + W_(-2));
-    if (p.nterms > 2) acc = acc + p.c3 * (W_(3) - ur - ur + W_(-3)) + p.c4 * (W_(4) - ur - ur + W_(-4));
-    return acc;
-  }
-#undef W_
-}
-
-// Warp-per-line solve: lane t owns rows t*L .. t*L+L-1 of a 32*L line; the
-// chunk carries are an inclusive cyclic Kogge-Stone scan over the lanes.
-template <int KIND, int L>
-__device__ __forceinline__ void circ_warp(const float* w, float* v, const CircOp& p, int lane) {
-  constexpr int LO = Halo<KIND>::lo;
-  constexpr unsigned FULL = 0xffffffffu;
-#pragma unroll
-  for (int k = 0; k < L; ++k) v[k] = circ_rhs<KIND, LO>(w, k, p);
-#pragma unroll
-  for (int k = 1; k < L; ++k) v[k] = fmaf(p.nmu, v[k - 1], v[k]);
-  float b = v[L - 1];
-#pragma unroll
-  for (int s = 0; s < 5; ++s) b = fmaf(p.ak[s], __shfl_sync(FULL, b, (lane - (1 << s)) & 31), b);
-  const float cf = __shfl_sync(FULL, b, (lane + 31) & 31);
-#pragma unroll
-  for (int k = 0; k < L; ++k) v[k] = fmaf(p.pw[k], cf, v[k]);
-#pragma unroll
-  for (int k = L - 2; k >= 0; --k) v[k] = fmaf(p.nmu, v[k + 1], v[k]);
-  b = v[0];
-#pragma unroll
-  for (int s = 0; s < 5; ++s) b = fmaf(p.ak[s], __shfl_sync(FULL, b, (lane + (1 << s)) & 31), b);
-  const float cb = __shfl_sync(FULL, b, (lane + 1) & 31);
-#pragma unroll
-  for (int k = 0; k < L; ++k) v[k] = fmaf(p.qw[k], cb, v[k]);
-}
-
-// Asynchronous 4-byte global -> shared copy (LDGSTS): the copies are in
-// flight together and hold no registers.
-__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int PENDING>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
-}
 
 struct CdArgs {
   const float *ua, *uq, *a1;  // u_j, u_q, running sum (may be null / alias out)
@@ -118,14 +38,6 @@ struct CdArgs {
 // so the window of lane t is (L+1)(t+1) + d + floor(d/L) for row t*L + d:
 // compile-time offsets from one base, and a stride of L+1 (odd) across the
 // lanes, free of bank conflicts.
-template <int L>
-__host__ __device__ constexpr int xbuf() {
-  return 32 * L + L + 40;
-}
-template <int L>
-__device__ __forceinline__ constexpr int hoff(int d) {
-  return d + (d >= 0 ? d / L : -1);  // -L <= d < 2L
-}
 
 // Warps (lines) per block and blocks per SM: 4 x 5 = 20 warps, ~100 registers
 // per thread for the three solves of L = 16 rows without spills.
@@ -214,69 +126,6 @@ __global__ void __launch_bounds__(32 * XW, XB) conv_diff_x(const __grid_constant
 // order C, A, B) and out = a1 + r is written with a1 read in the epilogue.
 // Slab row r (-4 <= r < N+4), line c sits at (r + 4) * 18 + c: the chunks of a
 // half-warp (rows 8 apart: 8 * 18 = 16 mod 32 words) fall in disjoint banks.
-constexpr int YL = 8;     // rows per chunk
-constexpr int CP = 8;     // column pairs per block
-constexpr int SR2 = 18;   // slab row stride (floats)
-
-__device__ __forceinline__ float2 f2fma(float a, float2 b, float2 c) {
-  return make_float2(fmaf(a, b.x, c.x), fmaf(a, b.y, c.y));
-}
-__device__ __forceinline__ float2 f2fma2(float2 a, float2 b, float2 c) {
-  return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
-}
-
-template <int KIND, int LO>
-__device__ __forceinline__ float2 circ_rhs2(const float2* w, int k, const CircOp& p) {
-#define W_(d) w[k + LO + (d)]
-  if constexpr (KIND == K_DER1) {
-    return make_float2(p.c1 * (W_(1).x - W_(-1).x) + p.c2 * (W_(2).x - W_(-2).x),
-                       p.c1 * (W_(1).y - W_(-1).y) + p.c2 * (W_(2).y - W_(-2).y));
-  } else {
-    const float2 ur = W_(0);
-    float ax = p.c1 * (W_(1).x - ur.x - ur.x + W_(-1).x) + p.c2 * (W_(2).x - ur.x - ur.x + W_(-2).x);
-    float ay = p.c1 * (W_(1).y - ur.y - ur.y + W_(-1).y) + p.c2 * (W_(2).y - ur.y - ur.y + W_(-2).y);
-    if (p.nterms > 2) {
-      ax = ax + p.c3 * (W_(3).x - ur.x - ur.x + W_(-3).x) + p.c4 * (W_(4).x - ur.x - ur.x + W_(-4).x);
-      ay = ay + p.c3 * (W_(3).y - ur.y - ur.y + W_(-3).y) + p.c4 * (W_(4).y - ur.y - ur.y + W_(-4).y);
-    }
-    return make_float2(ax, ay);
-  }
-#undef W_
-}
-
-// Block solve of two lines per thread: thread (cp, ch) owns rows ch*L ..
-// ch*L+L-1 of lines 2cp and 2cp+1; FC chunks per line, carries through shared
-// memory (ef / eb: [FC][CP] float2).  Two block barriers; every thread of the
-// block must call it.
-template <int KIND, int L, int FC>
-__device__ __forceinline__ void circ_block2(const float2* w, float2* v, const CircOp& p, float2* ef, float2* eb,
-                                            int ch, int cp) {
-  constexpr int LO = Halo<KIND>::lo;
-#pragma unroll
-  for (int k = 0; k < L; ++k) v[k] = circ_rhs2<KIND, LO>(w, k, p);
-#pragma unroll
-  for (int k = 1; k < L; ++k) v[k] = f2fma(p.nmu, v[k - 1], v[k]);
-  ef[ch * CP + cp] = v[L - 1];
-  __syncthreads();
-  float2 c = make_float2(0.f, 0.f);
-  for (int j = p.J; j >= 1; --j) c = f2fma(p.Ach, c, ef[((ch - j) & (FC - 1)) * CP + cp]);
-#pragma unroll
-  for (int k = 0; k < L; ++k) v[k] = f2fma2(make_float2(p.pw[k], p.pw[k]), c, v[k]);
-#pragma unroll
-  for (int k = L - 2; k >= 0; --k) v[k] = f2fma(p.nmu, v[k + 1], v[k]);
-  eb[ch * CP + cp] = v[0];
-  __syncthreads();
-  c = make_float2(0.f, 0.f);
-  for (int j = p.J; j >= 1; --j) c = f2fma(p.Ach, c, eb[((ch + j) & (FC - 1)) * CP + cp]);
-#pragma unroll
-  for (int k = 0; k < L; ++k) v[k] = f2fma2(make_float2(p.qw[k], p.qw[k]), c, v[k]);
-}
-
-__device__ __forceinline__ void cp_async8(float* dst, const float* src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
-}
-
 template <int FC>
 __host__ __device__ constexpr size_t yz_smem() {
   return sizeof(float) * ((size_t)2 * (YL * FC + 8) * SR2 + (size_t)4 * FC * CP);
@@ -366,8 +215,8 @@ __global__ void __launch_bounds__(CP* FC, (CP * FC <= 512) ? 2 : 1) conv_diff_yz
 
 // ---- host side -------------------------------------------------------------
 // Circulant form of a periodic plan for chunks of L rows.
-static int fill_circ(const OpPlan* p, int L, int max_carries, CircOp& c) {
-  if (!p->periodic || p->nin != p->nout || (p->kind != K_DER1 && p->kind != K_DER2)) return X3D_ERR_UNSUPPORTED;
+int fill_circ(const OpPlan* p, int L, int max_carries, CircOp& c) {
+  if (!p->periodic || p->nin != p->nout) return X3D_ERR_UNSUPPORTED;
   const double al = p->alpha;
   if (!(4.0 * al * al < 1.0)) return X3D_ERR_UNSUPPORTED;  // not diagonally dominant
   const double mu = 2.0 * al / (1.0 + std::sqrt(1.0 - 4.0 * al * al));
@@ -377,7 +226,9 @@ static int fill_circ(const OpPlan* p, int L, int max_carries, CircOp& c) {
   c.c2 = (float)(p->cb * sc);
   c.c3 = (float)(p->cc * sc);
   c.c4 = (float)(p->cd * sc);
-  c.nterms = (p->kind == K_DER2 && p->cc == 0.0 && p->cd == 0.0) ? 2 : 4;
+  c.nterms = 4;
+  if (p->kind == K_DER2 && p->cc == 0.0 && p->cd == 0.0) c.nterms = 2;
+  if ((p->kind == K_IVP || p->kind == K_IPV) && p->cd == 0.0) c.nterms = 3;
   c.nmu = (float)(-mu);
   const double A = std::pow(-mu, L);
   c.Ach = (float)A;

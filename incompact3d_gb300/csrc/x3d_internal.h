@@ -159,6 +159,18 @@ int upload_plan(OpPlan* p);
 int rhs_axis_fast(Ctx* c, OpPlan* pA, OpPlan* pB, OpPlan* pC, float* out, const float* ua, const float* uq,
                   const float* a1, float nu, const int* dims, cudaStream_t st);
 bool rhs_axis_fast_ok(const Ctx* c, int axis, const int* dims);
+// Staggered operators of binary32 periodic lines in circulant form
+// (x3d_stag_circ.cu): one solve (x, y, z), the sum of two solves on two
+// inputs (y/z: deryvp + interyvp, interzvp + derzvp with FP64 output) and two
+// solves of one input (y/z: interzpv + derzpv, interypv + derypv).
+// X3D_ERR_UNSUPPORTED where stag_fast_ok is false or the pair is not one of
+// those.
+bool stag_fast_ok(const Ctx* c, int axis, const int* dims);
+int stag_one(Ctx* c, OpPlan* p, float* out, const float* in, const int* dims, cudaStream_t st);
+int stag_sum(Ctx* c, OpPlan* pA, const float* inA, OpPlan* pB, const float* inB, void* out, bool out64,
+             const int* dims, cudaStream_t st);
+int stag_dual(Ctx* c, OpPlan* pA, float* outA, OpPlan* pB, float* outB, const float* in, const int* dims,
+              cudaStream_t st);
 
 // Get (building on first use) the device plan of an operator.
 int get_plan(Ctx* c, int axis, int kind, int npaire, int coefset, OpPlan** out);

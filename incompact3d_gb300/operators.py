@@ -217,20 +217,31 @@ class Context:
         return rhs
 
     def divergence(self, ux, uy, uz, pp3=None):
+        """divergence of (ux, uy, uz) on the pressure mesh, FP64 result; binary32
+        velocity runs the FP32 operators (x3d_divergence_f32)."""
         torch = _torch()
         if pp3 is None:
             pp3 = torch.empty((self.nm[2], self.nm[1], self.nm[0]), dtype=torch.float64, device=ux.device)
-        check(self.lib.x3d_divergence(self.h, _ptr(pp3), _ptr(ux), _ptr(uy), _ptr(uz), _stream()),
-              "x3d_divergence")
+        fn = self.lib.x3d_divergence_f32 if ux.dtype == torch.float32 else self.lib.x3d_divergence
+        for t in (ux, uy, uz):
+            _dev(t, ux.dtype)
+        _dev(pp3, torch.float64)
+        check(fn(self.h, _ptr(pp3), _ptr(ux), _ptr(uy), _ptr(uz), _stream()), fn.__name__)
         return pp3
 
     def gradp(self, pp3, px=None, py=None, pz=None):
+        """gradient of pp3 on the velocity mesh in pp3's precision (FP32 runs
+        x3d_gradp_f32)."""
         torch = _torch()
         shp = (self.n[2], self.n[1], self.n[0])
-        px = torch.empty(shp, dtype=torch.float64, device=pp3.device) if px is None else px
-        py = torch.empty(shp, dtype=torch.float64, device=pp3.device) if py is None else py
-        pz = torch.empty(shp, dtype=torch.float64, device=pp3.device) if pz is None else pz
-        check(self.lib.x3d_gradp(self.h, _ptr(px), _ptr(py), _ptr(pz), _ptr(pp3), _stream()), "x3d_gradp")
+        dt = pp3.dtype
+        px = torch.empty(shp, dtype=dt, device=pp3.device) if px is None else px
+        py = torch.empty(shp, dtype=dt, device=pp3.device) if py is None else py
+        pz = torch.empty(shp, dtype=dt, device=pp3.device) if pz is None else pz
+        for t in (px, py, pz):
+            _dev(t, dt)
+        fn = self.lib.x3d_gradp_f32 if dt == torch.float32 else self.lib.x3d_gradp
+        check(fn(self.h, _ptr(px), _ptr(py), _ptr(pz), _ptr(pp3), _stream()), fn.__name__)
         return px, py, pz
 
     def cor_vel(self, ux, uy, uz, px, py, pz):

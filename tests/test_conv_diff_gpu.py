@@ -71,3 +71,33 @@ def test_conv_diff_is_refused_where_the_fused_kernel_does_not_apply(gpu_lib):
     u = torch.zeros((96, 96, 96), dtype=torch.float32, device="cuda")
     with pytest.raises(X3DError):
         ctx.conv_diff(1, 0, u, u, None, NU)
+
+
+# ---- staggered divergence / gradient in binary32 ---------------------------
+# divergence: the y and z sums are fused into the circulant solves; gradp: the
+# z and y pairs on one input.  Against the FP64 operators on the same (binary32
+# representable) inputs.  The FP32 chains differentiate binary32-rounded
+# intermediates (e.g. deryvp(interxvp(uy))), which amplifies their rounding by
+# about pi/dx, so the bound grows with n: divergence 5e-5 of the largest value
+# at n = 128, linear in n; gradient 7e-5 at n = 128, as n^1.5 (the x component
+# differentiates two interpolated intermediates).  The 96^3 case runs the
+# generic binary32 kernels and sits at the same level.
+@pytest.mark.parametrize("dims", [(128, 128, 128), (256, 256, 256), (512, 512, 512), (512, 256, 128),
+                                  (128, 512, 256), (96, 96, 96)])
+def test_divergence_and_gradp_f32_match_fp64(gpu_lib, dims):
+    import torch
+    nx, ny, nz = dims
+    shape = (nz, ny, nx)
+    ctx = gpu_lib.Context(nx, ny, nz, L, L, L)
+    u = [smooth(torch, shape, 30 + i).float() for i in range(3)]
+    tol = 5e-5 * max(dims) / 128
+    tolg = 7e-5 * (max(dims) / 128) ** 1.5
+    ref = ctx.divergence(*[t.double() for t in u])
+    div = ctx.divergence(*u)
+    assert relerr(div.cpu().numpy(), ref.cpu().numpy()) < tol, dims
+    p = smooth(torch, shape, 40).float()
+    gref = ctx.gradp(p.double())
+    g = ctx.gradp(p)
+    for a, b in zip(g, gref):
+        assert a.dtype == torch.float32
+        assert relerr(a.cpu().numpy(), b.cpu().numpy()) < tolg, dims
