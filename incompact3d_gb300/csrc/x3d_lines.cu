@@ -3,6 +3,8 @@
 // factors, device upload) and argument marshalling.
 #include <type_traits>
 
+#include <cstdint>
+
 #include "x3d_line_fast.cuh"
 
 namespace x3d {
@@ -191,6 +193,14 @@ int launch_line_op(Ctx* c, OpPlan* p, T* out, const T* in, const int* dims_in, c
   if (dims_in[p->axis] != p->nin) return X3D_ERR_SHAPE;
   const int up = upload_plan(p);
   if (up != X3D_OK) return up;
+  // binary32 periodic x lines without a fused load / store: one warp per line
+  // in circulant form (x3d_stag_circ.cu)
+  if (std::is_same<T, float>::value && p->axis == 0 && p->periodic && p->nin == p->nout && pp == nullptr &&
+      (fz == nullptr || (fz->in2 == nullptr && !fz->active)) && stag_fast_ok(c, 0, dims_in) &&
+      reinterpret_cast<uintptr_t>(out) % 16 == 0) {
+    const int rc = stag_one(c, p, (float*)out, (const float*)in, dims_in, st);
+    if (rc != X3D_ERR_UNSUPPORTED) return rc;
+  }
   if (std::is_same<T, float>::value && p->periodic && p->nin == p->nout && pp == nullptr && c->fast_lines &&
       p->nout % FCHUNKS == 0 && (p->nout / FCHUNKS == 8 || p->nout / FCHUNKS == 16 || p->nout / FCHUNKS == 32))
     return launch_fast(p, (float*)out, (const float*)in, dims_in, st, (const Fuse<float>*)fz);

@@ -186,6 +186,9 @@ static int run_x(const StArgs& a, dim3 g, cudaStream_t st) {
 template <int L>
 static int run_x_kind(int kind, const StArgs& a, dim3 g, cudaStream_t st) {
   switch (kind) {
+    case K_DER1: return run_x<L, K_DER1>(a, g, st);
+    case K_DER2: return run_x<L, K_DER2>(a, g, st);
+    case K_FIL: return run_x<L, K_FIL>(a, g, st);
     case K_DVP: return run_x<L, K_DVP>(a, g, st);
     case K_IVP: return run_x<L, K_IVP>(a, g, st);
     case K_DPV: return run_x<L, K_DPV>(a, g, st);

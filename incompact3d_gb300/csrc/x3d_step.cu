@@ -638,9 +638,9 @@ static int divergence(SolverImpl* s, const T* ux, const T* uy, const T* uz, doub
     RC(stag_one(c, xi, fy, (const float*)uy, d1, st));
     RC(stag_one(c, xi, fz, (const float*)uz, d1, st));
     RC(stag_sum(c, yd, fy, yi, f1, fd, false, d1, st));  // duy = deryvp(pgy1) + interyvp(pp1)
-    RC(stag_one(c, yi, fu, fz, d1, st));                 // upi2 = interyvp(pgz1)
+    RC(op<T>(s, 1, K_IVP, 1, upi2, pgz1, d1, st));       // upi2 = interyvp(pgz1)
     RC(stag_sum(c, zi, fd, zd, fu, pp64, true, d1, st)); // pp3 = interzvp(duy) + derzvp(upi2)
-    s->launches += 6;
+    s->launches += 5;
     return X3D_OK;
   }
   RC(op<T>(s, 0, K_DVP, 0, pp1, ux, d1, st));
@@ -682,14 +682,14 @@ static int gradp(SolverImpl* s, const T* pp3, T* px, T* py, T* pz, cudaStream_t 
     RC(get_plan(c, 1, K_IPV, 1, default_coefset(K_IPV, 1), &yi));
     RC(get_plan(c, 2, K_DPV, 1, default_coefset(K_DPV, 1), &zd));
     RC(get_plan(c, 2, K_IPV, 1, default_coefset(K_IPV, 1), &zi));
-    float *f3 = (float*)ppi3, *fz = (float*)pgz3, *f2 = (float*)ppi2, *fy = (float*)pgy2, *fzi = (float*)pgzi2;
-    RC(stag_dual(c, zi, f3, zd, fz, (const float*)pp3, d3, st));  // ppi3, pgz3
+    float *f3 = (float*)ppi3, *f2 = (float*)ppi2, *fy = (float*)pgy2, *fzi = (float*)pgzi2;
+    RC(stag_dual(c, zi, f3, zd, (float*)pgz3, (const float*)pp3, d3, st));  // ppi3, pgz3
     RC(stag_dual(c, yi, f2, yd, fy, f3, d3, st));                 // ppi2, pgy2
-    RC(stag_one(c, yi, fzi, fz, d3, st));                          // pgzi2
+    RC(op<T>(s, 1, K_IPV, 1, pgzi2, pgz3, d3, st));                // pgzi2
     RC(stag_one(c, xd, (float*)px, f2, d3, st));
     RC(stag_one(c, xi, (float*)py, fy, d3, st));
     RC(stag_one(c, xi, (float*)pz, fzi, d3, st));
-    s->launches += 6;
+    s->launches += 5;
     return X3D_OK;
   }
   RC(op<T>(s, 2, K_IPV, 1, ppi3, pp3, d3, st));
