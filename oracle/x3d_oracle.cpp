@@ -769,6 +769,18 @@ void setup_axis(Axis& a, int n, double len, int ncl1, int ncln, const Opts& o) {
   filter_coefficients(a, o.filter_alpha);
 }
 
+// Interpolation transfer function at rl = (mode wavenumber) * d, as the
+// kxyz assembly of waves writes it (src/poisson.f90:1740-1760).
+double transfer(const Axis& a, double rl) {
+  const double tt = 2.0 * (a.bici6 * std::cos(rl * 1.5) + a.cicoef6 * std::cos(rl * 2.5) + a.dici6 * std::cos(rl * 3.5));
+  const double tt1 = 2.0 * a.aici6 * std::cos(rl * 0.5);
+  const double t1 = 1.0 + 2.0 * a.ailcai6 * std::cos(rl);
+  return (tt1 + tt) / t1;
+}
+
+// Free-slip at both ends (ncl = 1 / 1).
+bool slip_axis(const Axis& a) { return a.ncl1 == 1 && a.ncln == 1; }
+
 // Modified wavenumbers of the staggered scheme and the interpolation transfer
 // functions: src/poisson.f90:1530-1810 (waves, periodic branches) and the
 // kxyz assembly at src/poisson.f90:1688-1724.
@@ -1874,6 +1886,241 @@ int ox_scalars(void* h, int axis, double* out) {
   return n;
 }
 
+// ---------------------------------------------------------------------------
+// Poisson solve with free-slip x and y (and z free-slip or periodic):
+// src/poisson.f90:1019-1465 (poisson_11x, istret = 0).  The p-mesh sizes
+// NX = nxm, NY = nym, NZ = nzm (nz if z is periodic); spectral array
+// (NX, NY, NZ/2+1) as 2DECOMP's PHYSICAL_IN_Z transform leaves it.
+// ---------------------------------------------------------------------------
+
+// Wavenumber^2 and interpolation transfer of the modes of a free-slip axis
+// (waves, bcx = 1 / bcy = 1: src/poisson.f90:1588-1601, 1621-1637; the
+// transfer of :1740-1760), m = 0..nm-1.
+void waves_slip(const Axis& a, vec& k2, vec& tr) {
+  const int nm = a.nm;
+  k2.assign(nm, 0.0);
+  tr.assign(nm, 0.0);
+  vec es(nm, 0.0);
+  for (int i = 1; i <= nm; ++i) {
+    const double w = TWOPI * 0.5 * (double)(i - 1) / (double)nm;
+    double wp = a.aci6 * 2.0 * a.d * std::sin(w * 0.5) + (a.bci6 * 2.0 * a.d) * std::sin(3.0 * 0.5 * w);
+    wp = wp / (1.0 + 2.0 * a.alcai6 * std::cos(w));
+    const double t = (double)nm * wp / a.len;
+    k2[i - 1] = t * t;
+    es[i - 1] = (double)nm * w / a.len;
+  }
+  k2[0] = 0.0;
+  es[0] = 0.0;
+  for (int i = 0; i < nm; ++i) tr[i] = transfer(a, es[i] * a.d);
+}
+
+// kxyz of poisson_11x (src/poisson.f90:1725-1806): (re, im) per spectral point
+// (i, j, k), i fastest, k < NZ/2+1.  For a periodic z both parts are equal.
+void kxyz_11x(const OxCtx& c, vec& kre, vec& kim) {
+  const Axis &ax = c.ax[0], &ay = c.ax[1], &az = c.ax[2];
+  const int NX = ax.nm, NY = ay.nm, NZ = az.nm, NZ2 = NZ / 2 + 1;
+  vec kx2, trx, ky2, try_;
+  waves_slip(ax, kx2, trx);
+  waves_slip(ay, ky2, try_);
+  kre.assign((size_t)NX * NY * NZ2, 0.0);
+  kim.assign(kre.size(), 0.0);
+  if (az.periodic) {
+    vec kz2, trz;
+    waves_axis(az, kz2, trz);
+    for (int k = 0; k < NZ2; ++k)
+      for (int j = 0; j < NY; ++j)
+        for (int i = 0; i < NX; ++i) {
+          const double txz = try_[j] * trz[k], tyz = trx[i] * trz[k], txy = trx[i] * try_[j];
+          const double xt2 = kx2[i] * (txz * txz), yt2 = ky2[j] * (tyz * tyz), zt2 = kz2[k] * (txy * txy);
+          const size_t q = (size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k);
+          kre[q] = xt2 + yt2 + zt2;
+          kim[q] = kre[q];
+        }
+    return;
+  }
+  // free-slip z: the real part carries mode k, the imaginary part mode NZ-k
+  for (int k = 1; k <= NZ2; ++k) {
+    const double w = PI * (double)(k - 1) / (double)NZ;
+    const double w1 = PI * (double)(NZ - k + 1) / (double)NZ;
+    double wp = az.aci6 * 2.0 * az.d * std::sin(w * 0.5) + (az.bci6 * 2.0 * az.d) * std::sin(3.0 * 0.5 * w);
+    wp = wp / (1.0 + 2.0 * az.alcai6 * std::cos(w));
+    double w1p = az.aci6 * 2.0 * az.d * std::sin(w1 * 0.5) + (az.bci6 * 2.0 * az.d) * std::sin(3.0 * 0.5 * w1);
+    w1p = w1p / (1.0 + 2.0 * az.alcai6 * std::cos(w1));
+    const double kzr = (double)NZ * wp / az.len, kzi = (double)NZ * w1p / az.len;
+    const double zk2r = kzr * kzr, zk2i = kzi * kzi;
+    const double rlezs = ((double)NZ * w / az.len) * az.d, iyezs = ((double)NZ * w1 / az.len) * az.d;
+    const double ztr = 2.0 * (az.bici6 * std::cos(rlezs * 1.5) + az.cicoef6 * std::cos(rlezs * 2.5) +
+                              az.dici6 * std::cos(rlezs * 3.5));
+    const double zti = 2.0 * (az.bici6 * std::cos(iyezs * 1.5) + az.cicoef6 * std::cos(iyezs * 2.5) +
+                              az.dici6 * std::cos(iyezs * 3.5));
+    const double zt1r = 2.0 * az.aici6 * std::cos(rlezs * 0.5), zt1i = 2.0 * az.aici6 * std::cos(iyezs * 0.5);
+    const double z1r = 1.0 + 2.0 * az.ailcai6 * std::cos(rlezs), z1i = 1.0 + 2.0 * az.ailcai6 * std::cos(iyezs);
+    const double t1r = (zt1r + ztr) / z1r, t1i = (zt1i + zti) / z1i;
+    for (int j = 0; j < NY; ++j)
+      for (int i = 0; i < NX; ++i) {
+        const double t2 = try_[j], t3 = trx[i];
+        const double t4r = t2 * t2 * (t1r * t1r), t4i = t2 * t2 * (t1i * t1i);
+        const double t5r = t3 * t3 * (t1r * t1r), t5i = t3 * t3 * (t1i * t1i);
+        const double t6 = (t3 * t2) * (t3 * t2);
+        const size_t q = (size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * (k - 1));
+        kre[q] = t4r * kx2[i] + t5r * ky2[j] + t6 * zk2r;
+        kim[q] = t4i * kx2[i] + t5i * ky2[j] + t6 * zk2i;
+      }
+  }
+}
+
+// even / odd reorder of one axis (src/poisson.f90:1041-1098): v[d] = u[p(d)]
+inline int slip_perm(int d, int n) { return (d < n / 2) ? 2 * d : 2 * n - 2 * d - 1; }
+
+static void poisson_11x(const OxCtx& c, double* rhs) {
+  const int NX = c.ax[0].nm, NY = c.ax[1].nm, NZ = c.ax[2].nm, NZ2 = NZ / 2 + 1;
+  const bool bcz = !c.ax[2].periodic;
+  const size_t N = (size_t)NX * NY * NZ;
+  {
+    vec t(rhs, rhs + N);
+    for (int k = 0; k < NZ; ++k)
+      for (int j = 0; j < NY; ++j)
+        for (int i = 0; i < NX; ++i)
+          rhs[idx3(i, j, k, NX, NY)] =
+              t[idx3(slip_perm(i, NX), slip_perm(j, NY), bcz ? slip_perm(k, NZ) : k, NX, NY)];
+  }
+  std::vector<cplx> cw((size_t)NX * NY * NZ2);
+  auto CW = [&](int i, int j, int k) -> cplx& { return cw[(size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k)]; };
+#pragma omp parallel
+  {
+    std::vector<cplx> line, work;
+#pragma omp for collapse(2)
+    for (int j = 0; j < NY; ++j)
+      for (int i = 0; i < NX; ++i) {
+        line.assign(NZ, cplx(0, 0));
+        for (int k = 0; k < NZ; ++k) line[k] = cplx(rhs[idx3(i, j, k, NX, NY)], 0.0);
+        fft1d(line.data(), NZ, -1, work);
+        for (int k = 0; k < NZ2; ++k) CW(i, j, k) = line[k];
+      }
+#pragma omp for collapse(2)
+    for (int k = 0; k < NZ2; ++k)
+      for (int i = 0; i < NX; ++i) {
+        line.resize(NY);
+        for (int j = 0; j < NY; ++j) line[j] = CW(i, j, k);
+        fft1d(line.data(), NY, -1, work);
+        for (int j = 0; j < NY; ++j) CW(i, j, k) = line[j];
+      }
+#pragma omp for collapse(2)
+    for (int k = 0; k < NZ2; ++k)
+      for (int j = 0; j < NY; ++j) {
+        line.resize(NX);
+        for (int i = 0; i < NX; ++i) line[i] = CW(i, j, k);
+        fft1d(line.data(), NX, -1, work);
+        for (int i = 0; i < NX; ++i) CW(i, j, k) = line[i];
+      }
+  }
+  for (auto& v : cw) v = cplx(v.real() / (double)NX / (double)NY / (double)NZ, v.imag() / (double)NX / (double)NY / (double)NZ);
+  vec sax, sbx, say, sby, saz, sbz;
+  abxyz_half(NX, sax, sbx);
+  abxyz_half(NY, say, sby);
+  if (bcz) abxyz_half(NZ, saz, sbz);
+  else abxyz_axis(NZ, saz, sbz);
+  // post-processing in z, y, x (src/poisson.f90:1117-1198)
+  for (int k = 0; k < NZ2; ++k)
+    for (int j = 0; j < NY; ++j)
+      for (int i = 0; i < NX; ++i) {
+        cplx& v = CW(i, j, k);
+        const double t1 = v.real(), t2 = v.imag();
+        v = cplx(t1 * sbz[k] + t2 * saz[k], t2 * sbz[k] - t1 * saz[k]);
+      }
+  auto pair_fwd = [](cplx a, cplx b, double bb, double aa) {
+    const double t1 = a.real(), t2 = a.imag(), t3 = b.real(), t4 = b.imag();
+    const double x1 = t1 * bb * 0.5, x2 = t1 * aa * 0.5, x3 = t2 * bb * 0.5, x4 = t2 * aa * 0.5;
+    const double x5 = t3 * bb * 0.5, x6 = t3 * aa * 0.5, x7 = t4 * bb * 0.5, x8 = t4 * aa * 0.5;
+    return cplx(x1 + x4 + x5 - x8, -x2 + x3 + x6 + x7);
+  };
+  auto pair_bwd = [](cplx a, cplx b, double bb, double aa) {
+    const double t1 = a.real(), t2 = a.imag(), t3 = b.real(), t4 = b.imag();
+    const double x1 = t1 * bb, x2 = t1 * aa, x3 = t2 * bb, x4 = t2 * aa;
+    const double x5 = t3 * bb, x6 = t3 * aa, x7 = t4 * bb, x8 = t4 * aa;
+    return cplx(x1 - x4 + x6 + x7, -(-x2 - x3 + x5 - x8));
+  };
+  std::vector<cplx> cb(cw.size());
+  auto CB = [&](int i, int j, int k) -> cplx& { return cb[(size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k)]; };
+  for (int k = 0; k < NZ2; ++k)
+    for (int i = 0; i < NX; ++i) {
+      CB(i, 0, k) = CW(i, 0, k);
+      for (int j = 1; j < NY; ++j) CB(i, j, k) = pair_fwd(CW(i, j, k), CW(i, NY - j, k), sby[j], say[j]);
+    }
+  for (int k = 0; k < NZ2; ++k)
+    for (int j = 0; j < NY; ++j) {
+      CW(0, j, k) = CB(0, j, k);
+      for (int i = 1; i < NX; ++i) CW(i, j, k) = pair_fwd(CB(i, j, k), CB(NX - i, j, k), sbx[i], sax[i]);
+    }
+  // division (src/poisson.f90:1200-1228)
+  vec kre, kim;
+  kxyz_11x(c, kre, kim);
+  const double eps = 1.0e-16;
+  for (size_t q = 0; q < cw.size(); ++q) {
+    const double t1 = kre[q], t2 = kim[q];
+    cplx& v = cw[q];
+    if (std::fabs(t1) < eps && std::fabs(t2) < eps) v = cplx(0.0, 0.0);
+    if (std::fabs(t1) < eps && std::fabs(t2) >= eps) v = cplx(0.0, v.imag() / (-t2));
+    if (std::fabs(t1) >= eps && std::fabs(t2) < eps) v = cplx(v.real() / (-t1), 0.0);
+    if (std::fabs(t1) >= eps && std::fabs(t2) >= eps) v = cplx(v.real() / (-t1), v.imag() / (-t2));
+  }
+  // backward post-processing in x, y, z (src/poisson.f90:1337-1411)
+  for (int k = 0; k < NZ2; ++k)
+    for (int j = 0; j < NY; ++j) {
+      CB(0, j, k) = CW(0, j, k);
+      for (int i = 1; i < NX; ++i) CB(i, j, k) = pair_bwd(CW(i, j, k), CW(NX - i, j, k), sbx[i], sax[i]);
+    }
+  for (int k = 0; k < NZ2; ++k)
+    for (int i = 0; i < NX; ++i) {
+      CW(i, 0, k) = CB(i, 0, k);
+      for (int j = 1; j < NY; ++j) CW(i, j, k) = pair_bwd(CB(i, j, k), CB(i, NY - j, k), sby[j], say[j]);
+    }
+  for (int k = 0; k < NZ2; ++k)
+    for (int j = 0; j < NY; ++j)
+      for (int i = 0; i < NX; ++i) {
+        cplx& v = CW(i, j, k);
+        const double t1 = v.real(), t2 = v.imag();
+        v = cplx(t1 * sbz[k] - t2 * saz[k], t2 * sbz[k] + t1 * saz[k]);
+      }
+  // c2r (x, y inverse, then z complex-to-real), then the inverse reorders
+  vec out(N);
+#pragma omp parallel
+  {
+    std::vector<cplx> line, work;
+#pragma omp for collapse(2)
+    for (int k = 0; k < NZ2; ++k)
+      for (int j = 0; j < NY; ++j) {
+        line.resize(NX);
+        for (int i = 0; i < NX; ++i) line[i] = CW(i, j, k);
+        fft1d(line.data(), NX, +1, work);
+        for (int i = 0; i < NX; ++i) CW(i, j, k) = line[i];
+      }
+#pragma omp for collapse(2)
+    for (int k = 0; k < NZ2; ++k)
+      for (int i = 0; i < NX; ++i) {
+        line.resize(NY);
+        for (int j = 0; j < NY; ++j) line[j] = CW(i, j, k);
+        fft1d(line.data(), NY, +1, work);
+        for (int j = 0; j < NY; ++j) CW(i, j, k) = line[j];
+      }
+#pragma omp for collapse(2)
+    for (int j = 0; j < NY; ++j)
+      for (int i = 0; i < NX; ++i) {
+        line.assign(NZ, cplx(0, 0));
+        for (int k = 0; k < NZ2; ++k) line[k] = CW(i, j, k);
+        for (int k = NZ2; k < NZ; ++k) line[k] = std::conj(CW(i, j, NZ - k));
+        line[0] = cplx(line[0].real(), 0.0);
+        if (NZ % 2 == 0) line[NZ / 2] = cplx(line[NZ / 2].real(), 0.0);
+        fft1d(line.data(), NZ, +1, work);
+        for (int k = 0; k < NZ; ++k) out[idx3(i, j, k, NX, NY)] = line[k].real();
+      }
+  }
+  for (int k = 0; k < NZ; ++k)
+    for (int j = 0; j < NY; ++j)
+      for (int i = 0; i < NX; ++i)
+        rhs[idx3(slip_perm(i, NX), slip_perm(j, NY), bcz ? slip_perm(k, NZ) : k, NX, NY)] = out[idx3(i, j, k, NX, NY)];
+}
+
 int ox_poisson(void* h, double* rhs) {
   const OxCtx* c = (const OxCtx*)h;
   if (c->ax[0].periodic && c->ax[1].periodic && c->ax[2].periodic) {
@@ -1883,6 +2130,11 @@ int ox_poisson(void* h, double* rhs) {
   if (c->ax[0].periodic && !c->ax[1].periodic && c->ax[2].periodic) {
     if (c->istret == 3) return -2;
     poisson_010(*c, rhs);
+    return 0;
+  }
+  if (slip_axis(c->ax[0]) && slip_axis(c->ax[1]) && (c->ax[2].periodic || slip_axis(c->ax[2]))) {
+    if (c->istret != 0) return -2;
+    poisson_11x(*c, rhs);
     return 0;
   }
   return -2;
@@ -1986,19 +2238,31 @@ int ox_tgv_stats(void* h, const double* ux, const double* uy, const double* uz, 
   apply3d(*c, 2, OP_DER1, 1, uy, th.data(), dims, nullptr);
   apply3d(*c, 2, OP_DER1, 0, uz, ti.data(), dims, nullptr);
   double enst = 0, eps = 0, eek = 0, eps2 = 0;
-  for (size_t m = 0; m < N; ++m) {
+  // sums over the points the reference visits: the last point of a free-slip
+  // axis is left out, and the mean is over nxc*nyc*nzc (nxc = nxm there;
+  // src/Case-TGV.f90:211-241)
+  const int sx = (c->ax[0].ncl1 == 1) ? c->nx - 1 : c->nx;
+  const int sy = (c->ax[1].ncl1 == 1) ? c->ny - 1 : c->ny;
+  const int sz = (c->ax[2].ncl1 == 1) ? c->nz - 1 : c->nz;
+  const double nc = (double)(c->ax[0].ncl1 == 1 ? c->ax[0].nm : c->nx) * (c->ax[1].ncl1 == 1 ? c->ax[1].nm : c->ny) *
+                    (c->ax[2].ncl1 == 1 ? c->ax[2].nm : c->nz);
+  auto box = [&](auto f) {
+    for (int k = 0; k < sz; ++k)
+      for (int j = 0; j < sy; ++j)
+        for (int i = 0; i < sx; ++i) f(idx3(i, j, k, c->nx, c->ny));
+  };
+  box([&](size_t m) {
     const double a1 = tf[m] - th[m], a2 = tg[m] - tc[m], a3 = tb[m] - td[m];
     enst = enst + 0.5 * (a1 * a1 + a2 * a2 + a3 * a3);
-  }
-  const double nc = (double)c->nx * c->ny * c->nz;
+  });
   enst = enst / nc;
-  for (size_t m = 0; m < N; ++m) {
+  box([&](size_t m) {
     const double s1 = 2.0 * ta[m], s2 = 2.0 * te[m], s3 = 2.0 * ti[m];
     const double s4 = td[m] + tb[m], s5 = tg[m] + tc[m], s6 = th[m] + tf[m];
     eps = eps + 0.5 * xnu * (s1 * s1 + s2 * s2 + s3 * s3 + 2.0 * (s4 * s4) + 2.0 * (s5 * s5) + 2.0 * (s6 * s6));
-  }
+  });
   eps = eps / nc;
-  for (size_t m = 0; m < N; ++m) eek = eek + 0.5 * (ux[m] * ux[m] + uy[m] * uy[m] + uz[m] * uz[m]);
+  box([&](size_t m) { eek = eek + 0.5 * (ux[m] * ux[m] + uy[m] * uy[m] + uz[m] * uz[m]); });
   eek = eek / nc;
   apply3d(*c, 0, OP_DER2, 0, ux, ta.data(), dims, nullptr);
   apply3d(*c, 0, OP_DER2, 1, uy, tb.data(), dims, nullptr);
@@ -2009,11 +2273,11 @@ int ox_tgv_stats(void* h, const double* ux, const double* uy, const double* uz, 
   apply3d(*c, 2, OP_DER2, 1, ux, tg.data(), dims, nullptr);
   apply3d(*c, 2, OP_DER2, 1, uy, th.data(), dims, nullptr);
   apply3d(*c, 2, OP_DER2, 0, uz, ti.data(), dims, nullptr);
-  for (size_t m = 0; m < N; ++m) {
+  box([&](size_t m) {
     const double di = (-xnu) * (ux[m] * (ta[m] + td[m] + tg[m]) + uy[m] * (tb[m] + te[m] + th[m]) +
                                 uz[m] * (tc[m] + tf[m] + ti[m]));
     eps2 = eps2 + di;
-  }
+  });
   eps2 = eps2 / nc;
   out[0] = eek; out[1] = eps; out[2] = eps2; out[3] = enst;
   return 0;
@@ -2078,7 +2342,7 @@ int ox_run(void* h, double* ux_, double* uy_, double* uz_, int nsteps, double dt
         }
       }
       divergence(*c, ux, uy, uz, pp3);
-      poisson_000(*c, pp3.data());
+      if (ox_poisson(h, pp3.data()) != 0) return -2;
       gradp(*c, pp3, px, py, pz);
       for (size_t m = 0; m < N; ++m) { ux[m] = ux[m] - px[m]; uy[m] = uy[m] - py[m]; uz[m] = uz[m] - pz[m]; }
     }
