@@ -21,6 +21,7 @@ Ctx::~Ctx() {
   }
   if (st.d_ppy) cudaFree(st.d_ppy);
   if (d_p010) cudaFree(d_p010);
+  if (d_p11) cudaFree(d_p11);
   for (void* t : d_inv)
     if (t) cudaFree(t);
   if (d_twid) cudaFree(d_twid);
@@ -460,6 +461,7 @@ int x3d_poisson(x3d_ctx* h, double* rhs, void* st) {
   if (!h || !rhs) return X3D_ERR_ARG;
   Ctx* c = C(h);
   if (c->ax[0].periodic && !c->ax[1].periodic && c->ax[2].periodic) return poisson_010(c, rhs, (cudaStream_t)st);
+  if (is_11x(c)) return poisson_11x(c, rhs, (cudaStream_t)st);
   return poisson_periodic(c, rhs, 0, (cudaStream_t)st);
 }
 int x3d_poisson_noalloc(x3d_ctx* h, double* rhs, void* st) {
@@ -471,6 +473,7 @@ int x3d_poisson_ex(x3d_ctx* h, double* rhs, int precision, void* st) {
   Ctx* c = C(h);
   if (c->ax[0].periodic && !c->ax[1].periodic && c->ax[2].periodic)
     return precision == 0 ? poisson_010(c, rhs, (cudaStream_t)st) : X3D_ERR_DTYPE;
+  if (is_11x(c)) return precision == 0 ? poisson_11x(c, rhs, (cudaStream_t)st) : X3D_ERR_DTYPE;
   return poisson_periodic(c, rhs, precision, (cudaStream_t)st);
 }
 

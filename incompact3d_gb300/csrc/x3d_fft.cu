@@ -1140,4 +1140,294 @@ int poisson_010(Ctx* c, double* rhs, cudaStream_t st) {
   return cuda_status(cudaGetLastError());
 }
 
+// ---------------------------------------------------------------------------
+// poisson_11x (src/poisson.f90:1019-1465): x and y free-slip, z free-slip
+// (bcz = 1) or periodic (bcz = 0), uniform mesh, FP64.  p-mesh NX x NY x NZ
+// (nxm, nym, nzm), spectrum NX x NY x (NZ/2+1) as 2DECOMP's PHYSICAL_IN_Z
+// transform leaves it.  The reference transforms the reordered field in 3-D,
+// then post-processes mode pairs (k, n-k) axis by axis, divides by kxyz, and
+// undoes the steps in reverse.  Each post-processing is a complex-linear map
+// along its own axis (a e + b conj(e)) / 2, so it commutes with the other
+// axes' transforms; here each axis is one kernel: gather (even / odd
+// reorder) + FFT + its post-processing, the x kernel also scales, divides
+// and runs the backward x steps, and the last kernel does the z
+// complex-to-real transform and the inverse reorder.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct P11 {
+  int NX, NY, NZ, NZ2, bcz;
+  const double2 *twx_f, *twx_i, *twy_f, *twy_i, *twz_f, *twz_i;
+  const double *sax, *sbx, *say, *sby, *saz, *sbz;
+  const double2* kxyz;
+};
+
+__device__ __forceinline__ int slip_perm(int d, int n) { return (d < n / 2) ? 2 * d : 2 * n - 2 * d - 1; }
+
+// forward mode-pair combination of src/poisson.f90:1138-1156, written as there
+__device__ __forceinline__ double2 p11_fwd(double2 a, double2 b, double bb, double aa) {
+  const double x1 = a.x * bb * 0.5, x2 = a.x * aa * 0.5, x3 = a.y * bb * 0.5, x4 = a.y * aa * 0.5;
+  const double x5 = b.x * bb * 0.5, x6 = b.x * aa * 0.5, x7 = b.y * bb * 0.5, x8 = b.y * aa * 0.5;
+  return make_double2(x1 + x4 + x5 - x8, -x2 + x3 + x6 + x7);
+}
+// backward combination of src/poisson.f90:1340-1356
+__device__ __forceinline__ double2 p11_bwd(double2 a, double2 b, double bb, double aa) {
+  const double x1 = a.x * bb, x2 = a.x * aa, x3 = a.y * bb, x4 = a.y * aa;
+  const double x5 = b.x * bb, x6 = b.x * aa, x7 = b.y * bb, x8 = b.y * aa;
+  return make_double2(x1 - x4 + x6 + x7, -(-x2 - x3 + x5 - x8));
+}
+
+enum { P11_ZF = 0, P11_YF = 1, P11_X = 2, P11_YB = 3, P11_ZB = 4 };
+
+// One kernel per stage; a block holds `lanes` lines of length n in shared
+// memory (buf) plus a second buffer for the mode-pair combination.
+template <int MODE>
+__global__ void __launch_bounds__(FFT_THREADS) k_p11(double2* __restrict__ W, double* __restrict__ rhs, P11 q,
+                                                     int lanes) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = (MODE == P11_X) ? q.NX : (MODE == P11_YF || MODE == P11_YB) ? q.NY : q.NZ;
+  const int ls = n + 1;
+  double2* buf = reinterpret_cast<double2*>(smem_raw);
+  double2* bf2 = buf + (size_t)lanes * ls;
+  const int NX = q.NX, NY = q.NY, NZ = q.NZ, NZ2 = q.NZ2;
+  const int a0 = blockIdx.x * lanes, b = blockIdx.y;
+  const int na = (MODE == P11_X) ? NY : NX;
+  const int nl = min(lanes, na - a0);
+  // spectral index of (line l, row r); lines are consecutive i (y, z stages)
+  // or consecutive j (x stage)
+  auto sidx = [&](int l, int r) -> size_t {
+    if (MODE == P11_X) return (size_t)r + (size_t)NX * ((size_t)(a0 + l) + (size_t)NY * b);
+    if (MODE == P11_YF || MODE == P11_YB) return (size_t)(a0 + l) + (size_t)NX * ((size_t)r + (size_t)NY * b);
+    return (size_t)(a0 + l) + (size_t)NX * ((size_t)b + (size_t)NY * r);
+  };
+  // ---- load
+  if (MODE == P11_ZF) {
+    const int j = b, pj = slip_perm(j, NY);
+    for (int e = threadIdx.x; e < lanes * n; e += FFT_THREADS) {
+      const int r = e / lanes, l = e - r * lanes;
+      if (l < nl) {
+        const int i = a0 + l, k = r;
+        const int pk = q.bcz ? slip_perm(k, NZ) : k;
+        buf[l * ls + r] = make_double2(rhs[(size_t)slip_perm(i, NX) + (size_t)NX * ((size_t)pj + (size_t)NY * pk)], 0.0);
+      }
+    }
+  } else if (MODE == P11_ZB) {
+    for (int e = threadIdx.x; e < lanes * NZ2; e += FFT_THREADS) {
+      const int r = e / lanes, l = e - r * lanes;
+      if (l < nl) {
+        const double2 v = W[sidx(l, r)];
+        // backward z combination (src/poisson.f90:1395-1404)
+        buf[l * ls + r] = make_double2(v.x * q.sbz[r] - v.y * q.saz[r], v.y * q.sbz[r] + v.x * q.saz[r]);
+      }
+    }
+    __syncthreads();
+    // Hermitian extension: complex-to-real along z
+    for (int e = threadIdx.x; e < lanes * n; e += FFT_THREADS) {
+      const int l = e / n, r = e - l * n;
+      if (l < nl) {
+        if (r >= NZ2) {
+          const double2 v = buf[l * ls + (n - r)];
+          buf[l * ls + r] = make_double2(v.x, -v.y);
+        }
+      }
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < nl; l += FFT_THREADS) {
+      buf[l * ls].y = 0.0;
+      if ((n & 1) == 0) buf[l * ls + n / 2].y = 0.0;
+    }
+  } else {
+    for (int e = threadIdx.x; e < lanes * n; e += FFT_THREADS) {
+      int l, r;
+      if (MODE == P11_X) { l = e / n; r = e - l * n; } else { r = e / lanes; l = e - r * lanes; }
+      if (l < nl) buf[l * ls + r] = W[sidx(l, r)];
+    }
+  }
+  __syncthreads();
+  // ---- pre-combination of the backward stages (x is done below)
+  if (MODE == P11_YB) {
+    for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
+      const int l = e / n, m = e - l * n;
+      bf2[l * ls + m] = (m == 0) ? buf[l * ls] : p11_bwd(buf[l * ls + m], buf[l * ls + n - m], q.sby[m], q.say[m]);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
+      const int l = e / n, m = e - l * n;
+      buf[l * ls + m] = bf2[l * ls + m];
+    }
+    __syncthreads();
+  }
+  // ---- transform
+  const double2 *twf = (MODE == P11_X) ? q.twx_f : (MODE == P11_YF || MODE == P11_YB) ? q.twy_f : q.twz_f;
+  const double2 *twi = (MODE == P11_X) ? q.twx_i : (MODE == P11_YF || MODE == P11_YB) ? q.twy_i : q.twz_i;
+  if (MODE == P11_ZF || MODE == P11_YF || MODE == P11_X) smem_fft<-1, double>(buf, ls, n, nl, twf);
+  else smem_fft<1, double>(buf, ls, n, nl, twi);
+  // ---- post-combination of the forward stages
+  if (MODE == P11_ZF) {
+    for (int e = threadIdx.x; e < nl * NZ2; e += FFT_THREADS) {
+      const int l = e / NZ2, k = e - l * NZ2;
+      const double2 v = buf[l * ls + k];
+      // src/poisson.f90:1117-1126
+      buf[l * ls + k] = make_double2(v.x * q.sbz[k] + v.y * q.saz[k], v.y * q.sbz[k] - v.x * q.saz[k]);
+    }
+    __syncthreads();
+  }
+  if (MODE == P11_YF) {
+    for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
+      const int l = e / n, m = e - l * n;
+      bf2[l * ls + m] = (m == 0) ? buf[l * ls] : p11_fwd(buf[l * ls + m], buf[l * ls + n - m], q.sby[m], q.say[m]);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
+      const int l = e / n, m = e - l * n;
+      buf[l * ls + m] = bf2[l * ls + m];
+    }
+    __syncthreads();
+  }
+  if (MODE == P11_X) {
+    const int k = b;
+    for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
+      const int l = e / n, m = e - l * n;
+      double2 v = (m == 0) ? buf[l * ls] : p11_fwd(buf[l * ls + m], buf[l * ls + n - m], q.sbx[m], q.sax[m]);
+      // normalisation (src/poisson.f90:1113-1114)
+      v = make_double2(v.x / (double)NX / (double)NY / (double)NZ, v.y / (double)NX / (double)NY / (double)NZ);
+      // division with the reference's guards (src/poisson.f90:1200-1224)
+      const double2 kk = q.kxyz[(size_t)m + (size_t)NX * ((size_t)(a0 + l) + (size_t)NY * k)];
+      const double eps = 1.0e-16;
+      const bool r0 = fabs(kk.x) < eps, i0 = fabs(kk.y) < eps;
+      if (r0 && i0) v = make_double2(0.0, 0.0);
+      else if (r0) v = make_double2(0.0, v.y / (-kk.y));
+      else if (i0) v = make_double2(v.x / (-kk.x), 0.0);
+      else v = make_double2(v.x / (-kk.x), v.y / (-kk.y));
+      bf2[l * ls + m] = v;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
+      const int l = e / n, m = e - l * n;
+      buf[l * ls + m] = (m == 0) ? bf2[l * ls] : p11_bwd(bf2[l * ls + m], bf2[l * ls + n - m], q.sbx[m], q.sax[m]);
+    }
+    __syncthreads();
+    smem_fft<1, double>(buf, ls, n, nl, q.twx_i);
+  }
+  // ---- store
+  if (MODE == P11_ZB) {
+    const int j = b, pj = slip_perm(j, NY);
+    for (int e = threadIdx.x; e < lanes * n; e += FFT_THREADS) {
+      const int r = e / lanes, l = e - r * lanes;
+      if (l < nl) {
+        const int i = a0 + l, k = r;
+        const int pk = q.bcz ? slip_perm(k, NZ) : k;
+        rhs[(size_t)slip_perm(i, NX) + (size_t)NX * ((size_t)pj + (size_t)NY * pk)] = buf[l * ls + r].x;
+      }
+    }
+  } else {
+    const int rows = (MODE == P11_ZF) ? NZ2 : n;
+    for (int e = threadIdx.x; e < lanes * rows; e += FFT_THREADS) {
+      int l, r;
+      if (MODE == P11_X) { l = e / rows; r = e - l * rows; } else { r = e / lanes; l = e - r * lanes; }
+      if (l < nl) W[sidx(l, r)] = buf[l * ls + r];
+    }
+  }
+}
+
+}  // namespace
+
+bool is_11x(const Ctx* c) {
+  auto slip = [](const AxisCoef& a) { return a.ncl1 == 1 && a.ncln == 1; };
+  return slip(c->ax[0]) && slip(c->ax[1]) && (c->ax[2].periodic || slip(c->ax[2]));
+}
+
+// Device tables of poisson_11x (one block of doubles):
+//   twx_f | twx_i (2 NX each) | twy_f | twy_i | twz_f | twz_i | sax | sbx (NX)
+//   | say | sby (NY) | saz | sbz (NZ) | kxyz (2 NX NY (NZ/2+1))
+static int p11_setup(Ctx* c) {
+  if (c->d_p11) return X3D_OK;
+  const AxisCoef &ax = c->ax[0], &ay = c->ax[1], &az = c->ax[2];
+  const int NX = ax.nm, NY = ay.nm, NZ = az.nm;
+  const double pi = std::acos(-1.0);
+  dvec h;
+  twiddles(NX, -1, h);
+  twiddles(NX, +1, h);
+  twiddles(NY, -1, h);
+  twiddles(NY, +1, h);
+  twiddles(NZ, -1, h);
+  twiddles(NZ, +1, h);
+  // abxyz (src/poisson.f90:1469-1526): half-cell factors of free-slip axes,
+  // the periodic factors for a periodic z
+  auto ab = [&](int n, bool slip) {
+    dvec a(n), bb(n);
+    for (int i = 1; i <= n; ++i) {
+      const double arg = slip ? (double)(i - 1) * pi * 0.5 / (double)n : (double)(i - 1) * pi / (double)n;
+      a[i - 1] = std::sin(arg);
+      bb[i - 1] = std::cos(arg);
+    }
+    h.insert(h.end(), a.begin(), a.end());
+    h.insert(h.end(), bb.begin(), bb.end());
+  };
+  ab(NX, true);
+  ab(NY, true);
+  ab(NZ, !az.periodic);
+  dvec kre, kim;
+  kxyz_11x(ax, ay, az, kre, kim);
+  for (size_t i = 0; i < kre.size(); ++i) {
+    h.push_back(kre[i]);
+    h.push_back(kim[i]);
+  }
+  double* d = nullptr;
+  if (cudaMalloc(&d, h.size() * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
+  cudaError_t e = cudaMemcpy(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(d);
+    return cuda_status(e);
+  }
+  c->d_p11 = d;
+  return X3D_OK;
+}
+
+int poisson_11x(Ctx* c, double* rhs, cudaStream_t st) {
+  if (!is_11x(c)) return X3D_ERR_BC;
+  if (c->st.istret != 0) return X3D_ERR_UNSUPPORTED;  // matrice_refinement path of poisson_11x
+  const int NX = c->ax[0].nm, NY = c->ax[1].nm, NZ = c->ax[2].nm, NZ2 = NZ / 2 + 1;
+  if (!pow2(NX) || !pow2(NY) || !pow2(NZ) || NX < 8 || NY < 8 || NZ < 8) return X3D_ERR_UNSUPPORTED;
+  if (NX > FFT_ELEMS || NY > FFT_ELEMS || NZ > FFT_ELEMS || NY > 65535 || NZ2 > 65535) return X3D_ERR_UNSUPPORTED;
+  int rc = p11_setup(c);
+  if (rc != X3D_OK) return rc;
+  const size_t need = (size_t)NX * NY * NZ2 * sizeof(double2);
+  if (c->fft_work_bytes < need) {
+    if (c->fft_work) cudaFree(c->fft_work);
+    c->fft_work = nullptr;
+    c->fft_work_bytes = 0;
+    if (cudaMalloc(&c->fft_work, need) != cudaSuccess) return X3D_ERR_NOMEM;
+    c->fft_work_bytes = need;
+  }
+  double2* W = reinterpret_cast<double2*>(c->fft_work);
+  P11 q;
+  q.NX = NX; q.NY = NY; q.NZ = NZ; q.NZ2 = NZ2; q.bcz = c->ax[2].periodic ? 0 : 1;
+  const double* t = c->d_p11;
+  const double2* tw = reinterpret_cast<const double2*>(t);
+  q.twx_f = tw; q.twx_i = tw + NX;
+  q.twy_f = tw + 2 * NX; q.twy_i = q.twy_f + NY;
+  q.twz_f = q.twy_i + NY; q.twz_i = q.twz_f + NZ;
+  const double* s = t + 2 * (2 * NX + 2 * NY + 2 * NZ);
+  q.sax = s; q.sbx = s + NX; s += 2 * NX;
+  q.say = s; q.sby = s + NY; s += 2 * NY;
+  q.saz = s; q.sbz = s + NZ; s += 2 * NZ;
+  q.kxyz = reinterpret_cast<const double2*>(s);
+  auto launch = [&](auto kern, int n, int na, int nb) -> int {
+    const int lanes = std::max(1, std::min(32, FFT_ELEMS / n));
+    const size_t smem = (size_t)2 * lanes * (n + 1) * sizeof(double2);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e);
+    const dim3 g((unsigned)((na + lanes - 1) / lanes), (unsigned)nb);
+    kern<<<g, FFT_THREADS, smem, st>>>(W, rhs, q, lanes);
+    return cuda_status(cudaGetLastError());
+  };
+  rc = launch(k_p11<P11_ZF>, NZ, NX, NY);
+  if (rc == X3D_OK) rc = launch(k_p11<P11_YF>, NY, NX, NZ2);
+  if (rc == X3D_OK) rc = launch(k_p11<P11_X>, NX, NY, NZ2);
+  if (rc == X3D_OK) rc = launch(k_p11<P11_YB>, NY, NX, NZ2);
+  if (rc == X3D_OK) rc = launch(k_p11<P11_ZB>, NZ, NX, NY);
+  return rc;
+}
+
 }  // namespace x3d

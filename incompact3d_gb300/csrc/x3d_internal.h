@@ -84,6 +84,9 @@ void coef_indices(const AxisCoef& a, int kind, int coefset, int* fi, int* si, in
 
 // Poisson tables (periodic): modified wavenumber^2 and interpolation transfer.
 void waves_tables(const AxisCoef& a, dvec& k2, dvec& tr);
+// poisson_11x: kxyz (re, im) per spectral point (i, j, k < NZ/2+1), x and y
+// free-slip, z free-slip or periodic (x3d_plan.cpp).
+void kxyz_11x(const AxisCoef& ax, const AxisCoef& ay, const AxisCoef& az, dvec& kre, dvec& kim);
 
 // Mesh stretching in y and its device copies.
 struct Stretch {
@@ -130,6 +133,7 @@ struct Ctx {
   size_t fft_work_bytes = 0;
   Stretch st;
   double* d_p010 = nullptr;  // poisson_010 tables (see x3d_fft.cu)
+  double* d_p11 = nullptr;   // poisson_11x tables (see x3d_fft.cu)
   double p010_xa[2] = {0, 0};  // stretching constants xa0, xa1 of matrice_refinement
   std::unique_ptr<Workspace> ws;
   ~Ctx();
@@ -139,6 +143,10 @@ struct Ctx {
 int stretch_device(Ctx* c, const double** out);
 // poisson_010 (x, z periodic; y non-periodic, stretched or not), FP64.
 int poisson_010(Ctx* c, double* rhs, cudaStream_t st);
+// poisson_11x (src/poisson.f90:1019-1465): x and y free-slip, z free-slip or
+// periodic, uniform mesh, FP64 (x3d_fft.cu).
+int poisson_11x(Ctx* c, double* rhs, cudaStream_t st);
+bool is_11x(const Ctx* c);
 
 // Device scratch of at least `bytes` bytes (contents undefined).
 int ctx_workspace(Ctx* c, size_t bytes, void** out);

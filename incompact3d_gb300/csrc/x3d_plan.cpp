@@ -503,4 +503,87 @@ void waves_tables(const AxisCoef& a, dvec& k2, dvec& tr) {
   }
 }
 
+// poisson_11x tables (src/poisson.f90:1530-1810 with bcx = bcy = 1, istret = 0):
+// the wavenumber^2 and transfer of the modes of a free-slip axis, and kxyz
+// as (re, im) per spectral point (i, j, k), i fastest, k < NZ/2+1.  For a
+// free-slip z the real part carries mode k and the imaginary part mode NZ-k;
+// for a periodic z both parts are equal.
+static double transfer_at(const AxisCoef& a, double rl) {
+  const double tt = 2.0 * (a.bici6 * std::cos(rl * 1.5) + a.cici6s * std::cos(rl * 2.5) + a.dici6 * std::cos(rl * 3.5));
+  const double tt1 = 2.0 * a.aici6 * std::cos(rl * 0.5);
+  const double t1 = 1.0 + 2.0 * a.ailcai6 * std::cos(rl);
+  return (tt1 + tt) / t1;
+}
+
+static void waves_slip(const AxisCoef& a, dvec& k2, dvec& tr) {
+  const int nm = a.nm;
+  const double twopi = 2.0 * std::acos(-1.0);
+  k2.assign(nm, 0.0);
+  tr.assign(nm, 0.0);
+  dvec es(nm, 0.0);
+  for (int i = 1; i <= nm; ++i) {
+    const double w = twopi * 0.5 * (double)(i - 1) / (double)nm;
+    double wp = a.aci6 * 2.0 * a.d * std::sin(w * 0.5) + (a.bci6 * 2.0 * a.d) * std::sin(3.0 * 0.5 * w);
+    wp = wp / (1.0 + 2.0 * a.alcai6 * std::cos(w));
+    const double t = (double)nm * wp / a.len;
+    k2[i - 1] = t * t;
+    es[i - 1] = (double)nm * w / a.len;
+  }
+  k2[0] = 0.0;
+  es[0] = 0.0;
+  for (int i = 0; i < nm; ++i) tr[i] = transfer_at(a, es[i] * a.d);
+}
+
+void kxyz_11x(const AxisCoef& ax, const AxisCoef& ay, const AxisCoef& az, dvec& kre, dvec& kim) {
+  const int NX = ax.nm, NY = ay.nm, NZ = az.nm, NZ2 = NZ / 2 + 1;
+  const double pi = std::acos(-1.0);
+  dvec kx2, trx, ky2, tyy;
+  waves_slip(ax, kx2, trx);
+  waves_slip(ay, ky2, tyy);
+  kre.assign((size_t)NX * NY * NZ2, 0.0);
+  kim.assign(kre.size(), 0.0);
+  if (az.periodic) {
+    dvec kz2, trz;
+    waves_tables(az, kz2, trz);
+    for (int k = 0; k < NZ2; ++k)
+      for (int j = 0; j < NY; ++j)
+        for (int i = 0; i < NX; ++i) {
+          const double txz = tyy[j] * trz[k], tyz = trx[i] * trz[k], txy = trx[i] * tyy[j];
+          const double xt2 = kx2[i] * (txz * txz), yt2 = ky2[j] * (tyz * tyz), zt2 = kz2[k] * (txy * txy);
+          const size_t q = (size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k);
+          kre[q] = xt2 + yt2 + zt2;
+          kim[q] = kre[q];
+        }
+    return;
+  }
+  for (int k = 1; k <= NZ2; ++k) {
+    const double w = pi * (double)(k - 1) / (double)NZ;
+    const double w1 = pi * (double)(NZ - k + 1) / (double)NZ;
+    double wp = az.aci6 * 2.0 * az.d * std::sin(w * 0.5) + (az.bci6 * 2.0 * az.d) * std::sin(3.0 * 0.5 * w);
+    wp = wp / (1.0 + 2.0 * az.alcai6 * std::cos(w));
+    double w1p = az.aci6 * 2.0 * az.d * std::sin(w1 * 0.5) + (az.bci6 * 2.0 * az.d) * std::sin(3.0 * 0.5 * w1);
+    w1p = w1p / (1.0 + 2.0 * az.alcai6 * std::cos(w1));
+    const double kzr = (double)NZ * wp / az.len, kzi = (double)NZ * w1p / az.len;
+    const double zk2r = kzr * kzr, zk2i = kzi * kzi;
+    const double rlezs = ((double)NZ * w / az.len) * az.d, iyezs = ((double)NZ * w1 / az.len) * az.d;
+    const double ztr = 2.0 * (az.bici6 * std::cos(rlezs * 1.5) + az.cici6s * std::cos(rlezs * 2.5) +
+                              az.dici6 * std::cos(rlezs * 3.5));
+    const double zti = 2.0 * (az.bici6 * std::cos(iyezs * 1.5) + az.cici6s * std::cos(iyezs * 2.5) +
+                              az.dici6 * std::cos(iyezs * 3.5));
+    const double zt1r = 2.0 * az.aici6 * std::cos(rlezs * 0.5), zt1i = 2.0 * az.aici6 * std::cos(iyezs * 0.5);
+    const double z1r = 1.0 + 2.0 * az.ailcai6 * std::cos(rlezs), z1i = 1.0 + 2.0 * az.ailcai6 * std::cos(iyezs);
+    const double t1r = (zt1r + ztr) / z1r, t1i = (zt1i + zti) / z1i;
+    for (int j = 0; j < NY; ++j)
+      for (int i = 0; i < NX; ++i) {
+        const double t2 = tyy[j], t3 = trx[i];
+        const double t4r = t2 * t2 * (t1r * t1r), t4i = t2 * t2 * (t1i * t1i);
+        const double t5r = t3 * t3 * (t1r * t1r), t5i = t3 * t3 * (t1i * t1i);
+        const double t6 = (t3 * t2) * (t3 * t2);
+        const size_t q = (size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * (k - 1));
+        kre[q] = t4r * kx2[i] + t5r * ky2[j] + t6 * zk2r;
+        kim[q] = t4i * kx2[i] + t5i * ky2[j] + t6 * zk2i;
+      }
+  }
+}
+
 }  // namespace x3d

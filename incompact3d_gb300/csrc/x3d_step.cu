@@ -152,11 +152,17 @@ __global__ void k_tgv_init(double* ux, double* uy, double* uz, int nx, int ny, i
 
 // Block partial sums for the TGV statistics; one value per block per quantity.
 // q: 0 = 0.5*sum(u^2+v^2+w^2); 1 = eps(strain); 2 = enstrophy; 3 = eps2
+// Sums of postprocess_tgv over the points i < sx, j < sy, k < sz (the last
+// point of a free-slip axis is left out, src/Case-TGV.f90:211-226).
 __global__ void k_stats(const double* ux, const double* uy, const double* uz, const double* const* g,
-                        const double* const* l, double xnu, long long n, double* part) {
+                        const double* const* l, double xnu, long long n, int nx, int ny, int sx, int sy, int sz,
+                        double* part) {
   __shared__ double sh[4][256];
   double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
   GRID_STRIDE(m, n) {
+    const long long pl = (long long)nx * ny;
+    const int k = (int)(m / pl), j = (int)((m - (long long)k * pl) / nx), i = (int)(m - (long long)k * pl - (long long)j * nx);
+    if (i >= sx || j >= sy || k >= sz) continue;
     const double u = ux[m], v = uy[m], w = uz[m];
     a0 += 0.5 * (u * u + v * v + w * w);
     // g: 0 du/dx 1 dv/dx 2 dw/dx 3 du/dy 4 dv/dy 5 dw/dy 6 du/dz 7 dv/dz 8 dw/dz
@@ -439,6 +445,7 @@ struct SolverImpl {
   int launches = 0;
   // channel case: walls in y (x, z periodic)
   bool walls = false;       // geometry: y non-periodic with ncl 2/2
+  bool slip = false;        // geometry: free-slip x and y, z free-slip or periodic (poisson_11x)
   bool cfr = false;         // constant flow rate control (channel_cfr)
   double cfr_target = 2.0 / 3.0, wrotation = 0.0;
   int spinup_time = 0;
@@ -971,6 +978,8 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
   RC(divergence<T>(s, u[0], u[1], u[2], s->pp64, st));
   if (s->walls) {
     RC(poisson_010(c, s->pp64, st));
+  } else if (s->slip) {
+    RC(poisson_11x(c, s->pp64, st));
   } else {
     // mixed: FP64-class Poisson solve in double-float arithmetic on the FP32 pipes
     RC(poisson_periodic(c, s->pp64, mixed ? 2 : 0, st));
@@ -1063,16 +1072,20 @@ int x3d_solver_create(x3d_ctx* ctx_, const x3d_solver_opts* o, x3d_solver** out)
   // channel geometry: x, z periodic, no-slip walls at both y ends
   const bool walls = c->ax[0].periodic && c->ax[2].periodic && !c->ax[1].periodic && c->ax[1].ncl1 == 2 &&
                      c->ax[1].ncln == 2;
-  if (!periodic && !walls) return X3D_ERR_BC;
+  // free-slip box (the reference's TGV test case): x and y free-slip, z free-slip or periodic
+  const bool slip = is_11x(c);
+  if (!periodic && !walls && !slip) return X3D_ERR_BC;
   if (o->itimescheme != 3 && o->itimescheme != 5) return X3D_ERR_UNSUPPORTED;
   if (o->precision != X3D_PREC_FP64 && o->precision != X3D_PREC_MIXED) return X3D_ERR_DTYPE;
-  if (walls && o->precision != X3D_PREC_FP64) return X3D_ERR_DTYPE;
+  if ((walls || slip) && o->precision != X3D_PREC_FP64) return X3D_ERR_DTYPE;
+  if (slip && c->st.istret != 0) return X3D_ERR_UNSUPPORTED;
   if (walls && c->st.istret == 3) return X3D_ERR_UNSUPPORTED;
   x3d_solver* s = new x3d_solver();
   SolverImpl* si = &s->impl;
   si->c = c;
   si->o = *o;
   si->walls = walls;
+  si->slip = slip;
   si->N = (long long)c->grid.nx * c->grid.ny * c->grid.nz;
   si->Np = (long long)c->ax[0].nm * c->ax[1].nm * c->ax[2].nm;
   const double dt = o->dt;
@@ -1441,13 +1454,21 @@ int x3d_solver_tgv_stats(x3d_solver* s, double* out, void* stream) {
     all.insert(all.end(), l.begin(), l.end());
     cudaMemcpyAsync(dg, all.data(), 18 * sizeof(double*), cudaMemcpyHostToDevice, st);
     const unsigned nb = std::min<unsigned>(4096, pw_blocks(c, si->N));
-    k_stats<<<nb, 256, 0, st>>>(si->ux, si->uy, si->uz, dg, dg + 9, si->o.xnu, si->N, si->part);
+    // statistics over the reference's points: nxc = nxm on a free-slip axis
+    int sub[3];
+    double nc = 1.0;
+    for (int a = 0; a < 3; ++a) {
+      const bool fs = (c->ax[a].ncl1 == 1);
+      sub[a] = fs ? dims[a] - 1 : dims[a];
+      nc *= fs ? (double)c->ax[a].nm : (double)dims[a];
+    }
+    k_stats<<<nb, 256, 0, st>>>(si->ux, si->uy, si->uz, dg, dg + 9, si->o.xnu, si->N, dims[0], dims[1], sub[0],
+                                sub[1], sub[2], si->part);
     cudaMemcpyAsync(si->hpart, si->part, (size_t)nb * 4 * sizeof(double), cudaMemcpyDeviceToHost, st);
     rc = cuda_status(cudaStreamSynchronize(st));
     double acc[4] = {0, 0, 0, 0};
     for (unsigned b = 0; b < nb; ++b)
       for (int q = 0; q < 4; ++q) acc[q] += si->hpart[(size_t)b * 4 + q];
-    const double nc = (double)si->N;
     out[0] = acc[0] / nc;
     out[1] = acc[1] / nc;
     out[2] = acc[3] / nc;
