@@ -233,11 +233,15 @@ int x3d_filz_f32(x3d_ctx* ctx, float* tz, const float* uz, int nx, int ny, int n
  *   x, z periodic, y walls       -> poisson_010, src/poisson.f90:665-1013
  *     (cosine transform in y; on a stretched mesh, istret 1 or 2, the two
  *     pentadiagonal systems of matrice_refinement, src/poisson.f90:1814-2113,
- *     solved as inversion5_v1, src/tools.f90:1225-1362).
+ *     solved as inversion5_v1, src/tools.f90:1225-1362);
+ *   x, y free-slip (ncl 1/1), z free-slip or periodic
+ *                                -> poisson_11x, src/poisson.f90:1019-1465
+ *     (uniform mesh; the even/odd reorders and half-cell cosine combinations
+ *     along x and y, and along z when it is free-slip).
  * rhs (nxm,nym,nzm) in device memory is overwritten by the solution.
  * precision (poisson_000 only): 0 = FP64 FFT, 1 = FP32 FFT, 2 = double-float
  * FFT (each real carried as a hi+lo pair of binary32, ~48-bit significand,
- * computed on the FP32 pipes).  poisson_010 runs in FP64. */
+ * computed on the FP32 pipes).  poisson_010 and poisson_11x run in FP64. */
 int x3d_poisson(x3d_ctx* ctx, double* rhs, void* stream);
 int x3d_poisson_ex(x3d_ctx* ctx, double* rhs, int precision, void* stream);
 
