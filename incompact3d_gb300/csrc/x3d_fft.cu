@@ -108,8 +108,11 @@ struct FTnative {
     return S < 0 ? C{(o.y - o.x) * h, -(o.x + o.y) * h} : C{-(o.x + o.y) * h, (o.x - o.y) * h};
   }
   static __device__ __forceinline__ C from(double re, double im) { return C{(R)re, (R)im}; }
+  static __device__ __forceinline__ C from_f(float re, float im) { return C{(R)re, (R)im}; }
   static __device__ __forceinline__ double re(C a) { return (double)a.x; }
   static __device__ __forceinline__ double im(C a) { return (double)a.y; }
+  static __device__ __forceinline__ float re_f(C a) { return (float)a.x; }
+  static __device__ __forceinline__ float im_f(C a) { return (float)a.y; }
   static __device__ __forceinline__ C zero() { return C{(R)0, (R)0}; }
 };
 template <>
@@ -148,8 +151,13 @@ struct FT<DF> {
                  : mk(df_neg(df_mul(df_add(x, y), h)), df_mul(df_sub(x, y), h));
   }
   static __device__ __forceinline__ C from(double re, double im) { return mk(df_from(re), df_from(im)); }
+  // binary32 values are exact hi parts: no binary64 arithmetic on the way in
+  static __device__ __forceinline__ C from_f(float re, float im) { return C{re, 0.f, im, 0.f}; }
   static __device__ __forceinline__ double re(C a) { return df_to(R_(a)); }
   static __device__ __forceinline__ double im(C a) { return df_to(I_(a)); }
+  // nearest binary32 of hi + lo (|lo| <= ulp(hi) / 2: one rounding)
+  static __device__ __forceinline__ float re_f(C a) { return __fadd_rn(a.rh, a.rl); }
+  static __device__ __forceinline__ float im_f(C a) { return __fadd_rn(a.ih, a.il); }
   static __device__ __forceinline__ C zero() { return C{0.f, 0.f, 0.f, 0.f}; }
 };
 
@@ -251,8 +259,8 @@ int strided_lanes(int n) {
 
 // ---- Pass A: x real-to-complex --------------------------------------------
 // Lines of nx reals -> nx/2+1 complex.  M = nx/2, packed z[m] = x[2m] + i x[2m+1].
-template <typename P>
-__global__ void __launch_bounds__(FFT_THREADS) fft_x_r2c(const double* __restrict__ in,
+template <typename P, typename TI = double>
+__global__ void __launch_bounds__(FFT_THREADS) fft_x_r2c(const TI* __restrict__ in,
                                                          typename Cx<P>::T* __restrict__ out, int nx, long long nlines,
                                                          int lpb, const typename Cx<P>::T* __restrict__ tw_half,
                                                          const typename Cx<P>::T* __restrict__ tw_full) {
@@ -263,10 +271,18 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_x_r2c(const double* __restric
   const int M = nx / 2, nxh = M + 1;
   const long long l0 = (long long)blockIdx.x * lpb;
   const int nl = (int)min((long long)lpb, nlines - l0);
-  const double2* src = reinterpret_cast<const double2*>(in + l0 * nx);
-  for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
-    const double2 d = src[e];  // (x[2m], x[2m+1]) of line e / M
-    buf[e] = F::from(d.x, d.y);
+  if (std::is_same<TI, float>::value) {
+    const float2* src = reinterpret_cast<const float2*>(in + l0 * nx);
+    for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
+      const float2 d = src[e];  // (x[2m], x[2m+1]) of line e / M
+      buf[e] = F::from_f(d.x, d.y);
+    }
+  } else {
+    const double2* src = reinterpret_cast<const double2*>(in + l0 * nx);
+    for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
+      const double2 d = src[e];
+      buf[e] = F::from(d.x, d.y);
+    }
   }
   __syncthreads();
   smem_fft<-1, P>(buf, M, M, nl, tw_half);
@@ -283,9 +299,9 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_x_r2c(const double* __restric
 }
 
 // ---- Pass E: x complex-to-real (unnormalised inverse) ----------------------
-template <typename P>
+template <typename P, typename TO = double>
 __global__ void __launch_bounds__(FFT_THREADS) fft_x_c2r(const typename Cx<P>::T* __restrict__ in,
-                                                         double* __restrict__ out, int nx, long long nlines, int lpb,
+                                                         TO* __restrict__ out, int nx, long long nlines, int lpb,
                                                          const typename Cx<P>::T* __restrict__ tw_half_inv,
                                                          const typename Cx<P>::T* __restrict__ tw_full) {
   typedef typename Cx<P>::T C;
@@ -307,10 +323,18 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_x_c2r(const typename Cx<P>::T
   }
   __syncthreads();
   smem_fft<1, P>(buf, M, M, nl, tw_half_inv);
-  double2* dst = reinterpret_cast<double2*>(out + l0 * nx);
-  for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
-    const C z = buf[e];
-    dst[e] = double2{F::re(z), F::im(z)};
+  if (std::is_same<TO, float>::value) {
+    float2* dst = reinterpret_cast<float2*>(out + l0 * nx);
+    for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
+      const C z = buf[e];
+      dst[e] = float2{F::re_f(z), F::im_f(z)};
+    }
+  } else {
+    double2* dst = reinterpret_cast<double2*>(out + l0 * nx);
+    for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
+      const C z = buf[e];
+      dst[e] = double2{F::re(z), F::im(z)};
+    }
   }
 }
 
@@ -537,8 +561,8 @@ static int fft_setup(Ctx* c) {
   return cuda_status(cudaGetLastError());
 }
 
-template <typename R>
-static int poisson_run(Ctx* c, double* rhs, cudaStream_t st) {
+template <typename R, typename TIO = double>
+static int poisson_run(Ctx* c, TIO* rhs, cudaStream_t st) {
   typedef typename Cx<R>::T C;
   const int nx = c->grid.nx, ny = c->grid.ny, nz = c->grid.nz;
   const int M = nx / 2, nxh = M + 1;
@@ -591,7 +615,7 @@ static int poisson_run(Ctx* c, double* rhs, cudaStream_t st) {
     const long long nlines = (long long)ny * nz;
     const int lpb = std::max(1, FFT_ELEMS / std::max(M, 1));
     const size_t smem = (size_t)lpb * M * sizeof(C);
-    auto k = fft_x_r2c<R>;
+    auto k = fft_x_r2c<R, TIO>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const unsigned nb = (unsigned)((nlines + lpb - 1) / lpb);
     k<<<nb, FFT_THREADS, smem, st>>>(rhs, spec, nx, nlines, lpb, twx_f, twx_full);
@@ -626,12 +650,28 @@ static int poisson_run(Ctx* c, double* rhs, cudaStream_t st) {
     const long long nlines = (long long)ny * nz;
     const int lpb = std::max(1, FFT_ELEMS / std::max(M, 1));
     const size_t smem = (size_t)lpb * M * sizeof(C);
-    auto k = fft_x_c2r<R>;
+    auto k = fft_x_c2r<R, TIO>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const unsigned nb = (unsigned)((nlines + lpb - 1) / lpb);
     k<<<nb, FFT_THREADS, smem, st>>>(spec, rhs, nx, nlines, lpb, twx_i, twx_full);
   }
   return cuda_status(cudaGetLastError());
+}
+
+static int periodic_shape_ok(const Ctx* c) {
+  const int nx = c->grid.nx, ny = c->grid.ny, nz = c->grid.nz;
+  if (!c->ax[0].periodic || !c->ax[1].periodic || !c->ax[2].periodic) return X3D_ERR_BC;
+  if (!pow2(nx) || !pow2(ny) || !pow2(nz) || nx < 16 || ny < 8 || nz < 8) return X3D_ERR_UNSUPPORTED;
+  if (nx / 2 > FFT_ELEMS || ny > FFT_ELEMS / 1 || nz > FFT_ELEMS) return X3D_ERR_UNSUPPORTED;
+  if ((long long)ny * nz > (1LL << 31) || ny > 65535 || nz > 65535) return X3D_ERR_UNSUPPORTED;
+  return X3D_OK;
+}
+
+int poisson_periodic_f32io(Ctx* c, float* p, cudaStream_t st) {
+  int rc = periodic_shape_ok(c);
+  if (rc == X3D_OK) rc = fft_setup(c);
+  if (rc != X3D_OK) return rc;
+  return poisson_run<DF, float>(c, p, st);
 }
 
 int poisson_periodic(Ctx* c, double* rhs, int precision, cudaStream_t st) {

@@ -146,6 +146,9 @@ int poisson_010(Ctx* c, double* rhs, cudaStream_t st);
 // poisson_11x (src/poisson.f90:1019-1465): x and y free-slip, z free-slip or
 // periodic, uniform mesh, FP64 (x3d_fft.cu).
 int poisson_11x(Ctx* c, double* rhs, cudaStream_t st);
+// poisson_000 in double-float arithmetic on a binary32 right-hand side,
+// solution rounded once to binary32 in place (the mixed-precision step).
+int poisson_periodic_f32io(Ctx* c, float* p, cudaStream_t st);
 bool is_11x(const Ctx* c);
 
 // Device scratch of at least `bytes` bytes (contents undefined).

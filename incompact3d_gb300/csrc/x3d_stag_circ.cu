@@ -297,6 +297,7 @@ int stag_sum(Ctx* c, OpPlan* pA, const float* inA, OpPlan* pB, const float* inB,
   a.out0 = out;
   if (pA->kind == K_DVP && pB->kind == K_IVP && !out64) return run_yz_fc<K_DVP, K_IVP, SM_SUM, false>(FC, a, g, st);
   if (pA->kind == K_IVP && pB->kind == K_DVP && out64) return run_yz_fc<K_IVP, K_DVP, SM_SUM, true>(FC, a, g, st);
+  if (pA->kind == K_IVP && pB->kind == K_DVP && !out64) return run_yz_fc<K_IVP, K_DVP, SM_SUM, false>(FC, a, g, st);
   return X3D_ERR_UNSUPPORTED;
 }
 

@@ -439,7 +439,8 @@ struct SolverImpl {
   // work fields in operator precision
   void* W[16] = {nullptr};
   void* P[8] = {nullptr};  // pressure-mesh / intermediate-mesh work
-  double* pp64 = nullptr;
+  double* pp64 = nullptr;    // pressure (FP64 solvers)
+  float* p32 = nullptr;      // pressure of the mixed-precision solver (binary32)
   double* part = nullptr;  // reduction partials
   double* hpart = nullptr;
   int launches = 0;
@@ -622,7 +623,8 @@ static int momentum_rhs(SolverImpl* s, const T* const* u, T* const* H, cudaStrea
 // divergence (nlock=1) of src/navier.f90:257-372: pp64 = div(u) on the
 // pressure mesh, computed in T, written in FP64 for the Poisson solve.
 template <typename T>
-static int divergence(SolverImpl* s, const T* ux, const T* uy, const T* uz, double* pp64, cudaStream_t st) {
+static int divergence(SolverImpl* s, const T* ux, const T* uy, const T* uz, void* pout, bool out64,
+                      cudaStream_t st) {
   Ctx* c = s->c;
   const int nx = c->grid.nx, ny = c->grid.ny, nz = c->grid.nz;
   const int nxm = c->ax[0].nm, nym = c->ax[1].nm;
@@ -646,7 +648,7 @@ static int divergence(SolverImpl* s, const T* ux, const T* uy, const T* uz, doub
     RC(stag_one(c, xi, fz, (const float*)uz, d1, st));
     RC(stag_sum(c, yd, fy, yi, f1, fd, false, d1, st));  // duy = deryvp(pgy1) + interyvp(pp1)
     RC(op<T>(s, 1, K_IVP, 1, upi2, pgz1, d1, st));       // upi2 = interyvp(pgz1)
-    RC(stag_sum(c, zi, fd, zd, fu, pp64, true, d1, st)); // pp3 = interzvp(duy) + derzvp(upi2)
+    RC(stag_sum(c, zi, fd, zd, fu, pout, out64, d1, st)); // pp3 = interzvp(duy) + derzvp(upi2)
     s->launches += 5;
     return X3D_OK;
   }
@@ -663,7 +665,8 @@ static int divergence(SolverImpl* s, const T* ux, const T* uy, const T* uz, doub
   const int d3[3] = {nxm, nym, nz};
   RC(op<T>(s, 2, K_IVP, 1, pp3, duy, d3, st));
   RC(op<T>(s, 2, K_DVP, 0, po3, upi2, d3, st));
-  k_add_to64<T><<<pw_blocks(c, s->Np), 256, 0, st>>>(pp64, pp3, po3, s->Np);
+  if (out64) k_add_to64<T><<<pw_blocks(c, s->Np), 256, 0, st>>>((double*)pout, pp3, po3, s->Np);
+  else k_add<T><<<pw_blocks(c, s->Np), 256, 0, st>>>((T*)pout, pp3, po3, s->Np);
   s->launches++;
   return cuda_status(cudaGetLastError());
 }
@@ -975,23 +978,25 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
     s->launches++;
   }
   // projection: divergence, Poisson, gradient, correction
-  RC(divergence<T>(s, u[0], u[1], u[2], s->pp64, st));
-  if (s->walls) {
-    RC(poisson_010(c, s->pp64, st));
-  } else if (s->slip) {
-    RC(poisson_11x(c, s->pp64, st));
+  T** w = reinterpret_cast<T**>(s->W);
+  const T* pin = (const T*)s->pp64;
+  if (mixed) {
+    // binary32 divergence -> FP64-class Poisson solve in double-float
+    // arithmetic on the FP32 pipes -> binary32 pressure (rounded once)
+    RC(divergence<T>(s, u[0], u[1], u[2], s->p32, false, st));
+    RC(poisson_periodic_f32io(c, s->p32, st));
+    pin = (const T*)s->p32;
   } else {
-    // mixed: FP64-class Poisson solve in double-float arithmetic on the FP32 pipes
-    RC(poisson_periodic(c, s->pp64, mixed ? 2 : 0, st));
+    RC(divergence<T>(s, u[0], u[1], u[2], s->pp64, true, st));
+    if (s->walls) {
+      RC(poisson_010(c, s->pp64, st));
+    } else if (s->slip) {
+      RC(poisson_11x(c, s->pp64, st));
+    } else {
+      RC(poisson_periodic(c, s->pp64, 0, st));
+    }
   }
   s->launches += 5;
-  const T* pin = (const T*)s->pp64;
-  T** w = reinterpret_cast<T**>(s->W);
-  if (mixed) {
-    k_to32<<<pw_blocks(c, s->Np), 256, 0, st>>>((float*)w[4], s->pp64, s->Np);
-    s->launches++;
-    pin = (const T*)w[4];
-  }
   RC(gradp<T>(s, pin, w[0], w[1], w[2], st));
   if (s->walls) {
     k_wallgrad<<<pw_blocks(c, (long long)c->grid.nx * c->grid.nz), 256, 0, st>>>(
@@ -1052,9 +1057,15 @@ static int solver_alloc(SolverImpl* s) {
     s->P[k] = s->alloc<unsigned char>(N * (long long)es);
     if (!s->P[k]) return X3D_ERR_NOMEM;
   }
-  s->pp64 = s->alloc<double>(N);
+  if (mixed) {
+    s->p32 = s->alloc<float>(N);
+    if (!s->p32) return X3D_ERR_NOMEM;
+  } else {
+    s->pp64 = s->alloc<double>(N);
+    if (!s->pp64) return X3D_ERR_NOMEM;
+  }
   s->part = s->alloc<double>(4LL * 4096);
-  if (!s->pp64 || !s->part) return X3D_ERR_NOMEM;
+  if (!s->part) return X3D_ERR_NOMEM;
   if (cudaMallocHost(&s->hpart, 4 * 4096 * sizeof(double)) != cudaSuccess) return X3D_ERR_NOMEM;
   return cuda_status(cudaGetLastError());
 }
@@ -1315,7 +1326,8 @@ static int state_slot(SolverImpl* si, int which, void** ptr, long long* n, bool*
     return X3D_OK;
   }
   if (which == 9) {
-    *ptr = si->pp64;
+    *ptr = si->mixed() ? (void*)si->p32 : (void*)si->pp64;
+    *f32 = si->mixed();
     *n = si->Np;
     return X3D_OK;
   }
@@ -1495,7 +1507,7 @@ int x3d_solver_divmax(x3d_solver* s, double* out, void* stream) {
   std::memcpy(saveP, si->P, sizeof(saveP));
   for (int k = 0; k < 7; ++k) si->P[k] = P[k];
   double* dv = tmp + (size_t)7 * si->N;
-  int rc = divergence<double>(si, si->ux, si->uy, si->uz, dv, st);
+  int rc = divergence<double>(si, si->ux, si->uy, si->uz, dv, true, st);
   std::memcpy(si->P, saveP, sizeof(saveP));
   if (rc == X3D_OK) {
     const unsigned nb = std::min<unsigned>(4096, pw_blocks(c, si->Np));
@@ -1528,7 +1540,7 @@ int x3d_divergence(x3d_ctx* h, double* pp3, const double* ux, const double* uy, 
   int rc = ctx_workspace(c, (size_t)7 * s.N * sizeof(double), &ws);
   if (rc != X3D_OK) return rc;
   for (int k = 0; k < 7; ++k) s.P[k] = (double*)ws + (size_t)k * s.N;
-  return divergence<double>(&s, ux, uy, uz, pp3, (cudaStream_t)stream);
+  return divergence<double>(&s, ux, uy, uz, pp3, true, (cudaStream_t)stream);
 }
 
 int x3d_gradp(x3d_ctx* h, double* px, double* py, double* pz, const double* pp3, void* stream) {
@@ -1556,7 +1568,7 @@ int x3d_divergence_f32(x3d_ctx* h, double* pp3, const float* ux, const float* uy
   int rc = ctx_workspace(c, (size_t)7 * s.N * sizeof(float), &ws);
   if (rc != X3D_OK) return rc;
   for (int k = 0; k < 7; ++k) s.P[k] = (float*)ws + (size_t)k * s.N;
-  return divergence<float>(&s, ux, uy, uz, pp3, (cudaStream_t)stream);
+  return divergence<float>(&s, ux, uy, uz, pp3, true, (cudaStream_t)stream);
 }
 
 int x3d_gradp_f32(x3d_ctx* h, float* px, float* py, float* pz, const float* pp3, void* stream) {
