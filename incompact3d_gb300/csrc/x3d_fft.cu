@@ -201,12 +201,18 @@ __device__ __forceinline__ void fft8(C* v) {
 }
 
 // One Stockham pass of radix R over `nl` lines of length n held in smem
-// (line l at buf + l*lstride).  tw[m] = exp(SIGN*2*pi*i*m/n).
+// (line l at buf + l*lstride).  tw[m] = exp(SIGN*2*pi*i*m/n).  n, R and Ns
+// are powers of two (ln = log2 n, lns = log2 Ns): index arithmetic by shifts
+// and masks.
 template <int R, int SIGN, typename P, typename C>
-__device__ __forceinline__ void stockham_pass(C* buf, int lstride, int n, int nl, int Ns, const C* tw) {
+__device__ __forceinline__ void stockham_pass(C* buf, int lstride, int n, int ln, int nl, int Ns, int lns,
+                                              const C* tw) {
   constexpr int G = FFT_VALS / R;  // butterflies per thread
-  const int per_line = n / R;
+  constexpr int LR = (R == 8) ? 3 : (R == 4) ? 2 : 1;
+  const int lpl = ln - LR;  // log2(per_line)
+  const int per_line = 1 << lpl;
   const int total = per_line * nl;
+  const int lstep = ln - lns - LR;  // log2(n / (Ns R))
   C v[G][R];
   int base[G];
 #pragma unroll
@@ -214,20 +220,19 @@ __device__ __forceinline__ void stockham_pass(C* buf, int lstride, int n, int nl
     const int bt = threadIdx.x + g * FFT_THREADS;
     base[g] = -1;
     if (bt < total) {
-      const int l = bt / per_line, j = bt - l * per_line;
+      const int l = bt >> lpl, j = bt & (per_line - 1);
       C* line = buf + l * lstride;
-      const int kk = j % Ns;
-      const int step = n / (Ns * R);
+      const int kk = j & (Ns - 1);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         C x = line[j + r * per_line];
-        if (r > 0 && kk > 0) x = FT<P>::mul(x, tw[(kk * r * step) % n]);
+        if (r > 0 && kk > 0) x = FT<P>::mul(x, tw[((kk * r) << lstep) & (n - 1)]);
         v[g][r] = x;
       }
       if (R == 8) fft8<SIGN, P>(v[g]);
       if (R == 4) fft4<SIGN, P>(v[g][0], v[g][1], v[g][2], v[g][3]);
       if (R == 2) fft2<SIGN, P>(v[g][0], v[g][1]);
-      base[g] = l * lstride + (j / Ns) * Ns * R + kk;
+      base[g] = l * lstride + ((j >> lns) << (lns + LR)) + kk;
     }
   }
   __syncthreads();
@@ -242,12 +247,14 @@ __device__ __forceinline__ void stockham_pass(C* buf, int lstride, int n, int nl
 
 template <int SIGN, typename P, typename C>
 __device__ void smem_fft(C* buf, int lstride, int n, int nl, const C* tw) {
-  // nl * n <= FFT_ELEMS: one radix group of FFT_VALS values per thread
-  int Ns = 1;
+  // nl * n <= FFT_ELEMS: one radix group of FFT_VALS values per thread; n a
+  // power of two
+  const int ln = __ffs(n) - 1;
+  int Ns = 1, lns = 0;
   int rem = n;
-  while (rem >= 8) { stockham_pass<8, SIGN, P>(buf, lstride, n, nl, Ns, tw); Ns *= 8; rem /= 8; }
-  if (rem == 4) { stockham_pass<4, SIGN, P>(buf, lstride, n, nl, Ns, tw); Ns *= 4; rem /= 4; }
-  if (rem == 2) { stockham_pass<2, SIGN, P>(buf, lstride, n, nl, Ns, tw); }
+  while (rem >= 8) { stockham_pass<8, SIGN, P>(buf, lstride, n, ln, nl, Ns, lns, tw); Ns *= 8; lns += 3; rem >>= 3; }
+  if (rem == 4) { stockham_pass<4, SIGN, P>(buf, lstride, n, ln, nl, Ns, lns, tw); Ns *= 4; lns += 2; rem >>= 2; }
+  if (rem == 2) { stockham_pass<2, SIGN, P>(buf, lstride, n, ln, nl, Ns, lns, tw); }
 }
 
 // Lines per CTA of a strided pass: one radix group of values per thread
@@ -287,10 +294,14 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_x_r2c(const TI* __restrict__ 
   __syncthreads();
   smem_fft<-1, P>(buf, M, M, nl, tw_half);
   C* dst = out + l0 * nxh;
-  for (int e = threadIdx.x; e < nl * nxh; e += FFT_THREADS) {
-    const int l = e / nxh, k = e - l * nxh;
+  // M is a power of two: modes k = 0..M-1 by shift / mask, the k = M mode of
+  // each line after them
+  const int lm = __ffs(M) - 1;
+  for (int e = threadIdx.x; e < nl * (M + 1); e += FFT_THREADS) {
+    const bool last = e >= nl * M;
+    const int l = last ? e - nl * M : (e >> lm), k = last ? M : (e & (M - 1));
     const C* z = buf + l * M;
-    const C zk = z[k % M], zn = F::conj(z[(M - k) % M]);
+    const C zk = z[k & (M - 1)], zn = F::conj(z[(M - k) & (M - 1)]);
     // E = (Z[k] + conj Z[M-k])/2, O = (Z[k] - conj Z[M-k])/(2i), X = E + W^k O
     const C E = F::half(F::add(zk, zn));
     const C O = F::half(F::template mul_i<-1>(F::sub(zk, zn)));
@@ -312,8 +323,9 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_x_c2r(const typename Cx<P>::T
   const long long l0 = (long long)blockIdx.x * lpb;
   const int nl = (int)min((long long)lpb, nlines - l0);
   const C* src = in + l0 * nxh;
+  const int lm = __ffs(M) - 1;  // M a power of two
   for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
-    const int l = e / M, k = e - l * M;
+    const int l = e >> lm, k = e & (M - 1);
     const C xk = src[(long long)l * nxh + k];
     const C xn = F::conj(src[(long long)l * nxh + (M - k)]);
     // E = X[k] + conj X[M-k]; O = (X[k] - conj X[M-k]) * conj(W^k); Z = E + i O
@@ -458,8 +470,9 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_strided(typename Cx<P>::T* __
   const int nl = min(lanes, na - a0);
   const long long b = blockIdx.y;
   C* base = data + b * bs + a0;
+  const int llan = __ffs(lanes) - 1, lnn = __ffs(n) - 1;  // lanes, n: powers of two
   for (int e = threadIdx.x; e < lanes * n; e += FFT_THREADS) {
-    const int r = e / lanes, l = e - r * lanes;
+    const int r = e >> llan, l = e & (lanes - 1);
     if (l < nl) buf[l * lstride + r] = base[r * rs + l];
   }
   __syncthreads();
@@ -469,13 +482,13 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_strided(typename Cx<P>::T* __
     if (sp.inv) {
       const int nxh = sp.nx / 2 + 1;
       for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
-        const int l = e / n, kz = e - l * n;
+        const int l = e >> lnn, kz = e & (n - 1);
         const long long i = ((long long)kz * sp.ny + b) * nxh + a0 + l;
         buf[l * lstride + kz] = InvMul<P>::mul(buf[l * lstride + kz], sp.inv, i);
       }
     } else {
       for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
-        const int l = e / n, kz = e - l * n;
+        const int l = e >> lnn, kz = e & (n - 1);
         buf[l * lstride + kz] = Spectral<P>::apply(buf[l * lstride + kz], sp, a0 + l, (int)b, kz);
       }
     }
@@ -483,7 +496,7 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_strided(typename Cx<P>::T* __
     smem_fft<1, P>(buf, lstride, n, nl, tw_i);
   }
   for (int e = threadIdx.x; e < lanes * n; e += FFT_THREADS) {
-    const int r = e / lanes, l = e - r * lanes;
+    const int r = e >> llan, l = e & (lanes - 1);
     if (l < nl) base[r * rs + l] = buf[l * lstride + r];
   }
 }
