@@ -33,6 +33,14 @@ constexpr int FFT_THREADS = 512;
 constexpr int FFT_VALS = 8;  // complex values held per thread per pass
 constexpr int FFT_ELEMS = FFT_THREADS * FFT_VALS;  // complex values per CTA
 
+// Shared-memory line layout of the FFT kernels: element r of a line at
+// r + r/8 (one pad slot per 8 elements), lines fft_ls(n) apart.  A Stockham
+// pass writes 8 consecutive elements per thread; with the pad every store
+// instruction of a warp touches each bank quad at most 4 times (the minimum
+// for 16-byte elements) instead of 32.
+__host__ __device__ __forceinline__ int fft_pad(int r) { return r + (r >> 3); }
+__host__ __device__ __forceinline__ int fft_ls(int n) { return n + (n >> 3) + 1; }
+
 // ---------------------------------------------------------------------------
 // Arithmetic policies.  double / float: native complex arithmetic.  DF: every
 // real number is an unevaluated sum hi + lo of two binary32 numbers (about a
@@ -214,7 +222,7 @@ __device__ __forceinline__ void stockham_pass(C* buf, int lstride, int n, int ln
   const int total = per_line * nl;
   const int lstep = ln - lns - LR;  // log2(n / (Ns R))
   C v[G][R];
-  int base[G];
+  int base[G], off[G];
 #pragma unroll
   for (int g = 0; g < G; ++g) {
     const int bt = threadIdx.x + g * FFT_THREADS;
@@ -225,14 +233,15 @@ __device__ __forceinline__ void stockham_pass(C* buf, int lstride, int n, int ln
       const int kk = j & (Ns - 1);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        C x = line[j + r * per_line];
+        C x = line[fft_pad(j + r * per_line)];
         if (r > 0 && kk > 0) x = FT<P>::mul(x, tw[((kk * r) << lstep) & (n - 1)]);
         v[g][r] = x;
       }
       if (R == 8) fft8<SIGN, P>(v[g]);
       if (R == 4) fft4<SIGN, P>(v[g][0], v[g][1], v[g][2], v[g][3]);
       if (R == 2) fft2<SIGN, P>(v[g][0], v[g][1]);
-      base[g] = l * lstride + ((j >> lns) << (lns + LR)) + kk;
+      base[g] = l * lstride;
+      off[g] = ((j >> lns) << (lns + LR)) + kk;
     }
   }
   __syncthreads();
@@ -240,7 +249,7 @@ __device__ __forceinline__ void stockham_pass(C* buf, int lstride, int n, int ln
   for (int g = 0; g < G; ++g)
     if (base[g] >= 0) {
 #pragma unroll
-      for (int r = 0; r < R; ++r) buf[base[g] + r * Ns] = v[g][r];
+      for (int r = 0; r < R; ++r) buf[base[g] + fft_pad(off[g] + r * Ns)] = v[g][r];
     }
   __syncthreads();
 }
@@ -278,30 +287,29 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_x_r2c(const TI* __restrict__ 
   const int M = nx / 2, nxh = M + 1;
   const long long l0 = (long long)blockIdx.x * lpb;
   const int nl = (int)min((long long)lpb, nlines - l0);
+  const int lm = __ffs(M) - 1, ls = fft_ls(M);  // M a power of two
   if (std::is_same<TI, float>::value) {
     const float2* src = reinterpret_cast<const float2*>(in + l0 * nx);
     for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
       const float2 d = src[e];  // (x[2m], x[2m+1]) of line e / M
-      buf[e] = F::from_f(d.x, d.y);
+      buf[(e >> lm) * ls + fft_pad(e & (M - 1))] = F::from_f(d.x, d.y);
     }
   } else {
     const double2* src = reinterpret_cast<const double2*>(in + l0 * nx);
     for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
       const double2 d = src[e];
-      buf[e] = F::from(d.x, d.y);
+      buf[(e >> lm) * ls + fft_pad(e & (M - 1))] = F::from(d.x, d.y);
     }
   }
   __syncthreads();
-  smem_fft<-1, P>(buf, M, M, nl, tw_half);
+  smem_fft<-1, P>(buf, ls, M, nl, tw_half);
   C* dst = out + l0 * nxh;
-  // M is a power of two: modes k = 0..M-1 by shift / mask, the k = M mode of
-  // each line after them
-  const int lm = __ffs(M) - 1;
+  // modes k = 0..M-1 by shift / mask, the k = M mode of each line after them
   for (int e = threadIdx.x; e < nl * (M + 1); e += FFT_THREADS) {
     const bool last = e >= nl * M;
     const int l = last ? e - nl * M : (e >> lm), k = last ? M : (e & (M - 1));
-    const C* z = buf + l * M;
-    const C zk = z[k & (M - 1)], zn = F::conj(z[(M - k) & (M - 1)]);
+    const C* z = buf + l * ls;
+    const C zk = z[fft_pad(k & (M - 1))], zn = F::conj(z[fft_pad((M - k) & (M - 1))]);
     // E = (Z[k] + conj Z[M-k])/2, O = (Z[k] - conj Z[M-k])/(2i), X = E + W^k O
     const C E = F::half(F::add(zk, zn));
     const C O = F::half(F::template mul_i<-1>(F::sub(zk, zn)));
@@ -323,7 +331,7 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_x_c2r(const typename Cx<P>::T
   const long long l0 = (long long)blockIdx.x * lpb;
   const int nl = (int)min((long long)lpb, nlines - l0);
   const C* src = in + l0 * nxh;
-  const int lm = __ffs(M) - 1;  // M a power of two
+  const int lm = __ffs(M) - 1, ls = fft_ls(M);  // M a power of two
   for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
     const int l = e >> lm, k = e & (M - 1);
     const C xk = src[(long long)l * nxh + k];
@@ -331,20 +339,20 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_x_c2r(const typename Cx<P>::T
     // E = X[k] + conj X[M-k]; O = (X[k] - conj X[M-k]) * conj(W^k); Z = E + i O
     const C E = F::add(xk, xn);
     const C O = F::mul(F::sub(xk, xn), F::conj(tw_full[k]));
-    buf[l * M + k] = F::add(E, F::template mul_i<1>(O));
+    buf[l * ls + fft_pad(k)] = F::add(E, F::template mul_i<1>(O));
   }
   __syncthreads();
-  smem_fft<1, P>(buf, M, M, nl, tw_half_inv);
+  smem_fft<1, P>(buf, ls, M, nl, tw_half_inv);
   if (std::is_same<TO, float>::value) {
     float2* dst = reinterpret_cast<float2*>(out + l0 * nx);
     for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
-      const C z = buf[e];
+      const C z = buf[(e >> lm) * ls + fft_pad(e & (M - 1))];
       dst[e] = float2{F::re_f(z), F::im_f(z)};
     }
   } else {
     double2* dst = reinterpret_cast<double2*>(out + l0 * nx);
     for (int e = threadIdx.x; e < nl * M; e += FFT_THREADS) {
-      const C z = buf[e];
+      const C z = buf[(e >> lm) * ls + fft_pad(e & (M - 1))];
       dst[e] = double2{F::re(z), F::im(z)};
     }
   }
@@ -465,7 +473,7 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_strided(typename Cx<P>::T* __
   typedef typename Cx<P>::T C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
-  const int lstride = n + 1;
+  const int lstride = fft_ls(n);
   const int a0 = blockIdx.x * lanes;
   const int nl = min(lanes, na - a0);
   const long long b = blockIdx.y;
@@ -473,7 +481,7 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_strided(typename Cx<P>::T* __
   const int llan = __ffs(lanes) - 1, lnn = __ffs(n) - 1;  // lanes, n: powers of two
   for (int e = threadIdx.x; e < lanes * n; e += FFT_THREADS) {
     const int r = e >> llan, l = e & (lanes - 1);
-    if (l < nl) buf[l * lstride + r] = base[r * rs + l];
+    if (l < nl) buf[l * lstride + fft_pad(r)] = base[r * rs + l];
   }
   __syncthreads();
   smem_fft<SIGN, P>(buf, lstride, n, nl, SIGN < 0 ? tw_f : tw_i);
@@ -484,12 +492,12 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_strided(typename Cx<P>::T* __
       for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
         const int l = e >> lnn, kz = e & (n - 1);
         const long long i = ((long long)kz * sp.ny + b) * nxh + a0 + l;
-        buf[l * lstride + kz] = InvMul<P>::mul(buf[l * lstride + kz], sp.inv, i);
+        buf[l * lstride + fft_pad(kz)] = InvMul<P>::mul(buf[l * lstride + fft_pad(kz)], sp.inv, i);
       }
     } else {
       for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
         const int l = e >> lnn, kz = e & (n - 1);
-        buf[l * lstride + kz] = Spectral<P>::apply(buf[l * lstride + kz], sp, a0 + l, (int)b, kz);
+        buf[l * lstride + fft_pad(kz)] = Spectral<P>::apply(buf[l * lstride + fft_pad(kz)], sp, a0 + l, (int)b, kz);
       }
     }
     __syncthreads();
@@ -497,7 +505,7 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_strided(typename Cx<P>::T* __
   }
   for (int e = threadIdx.x; e < lanes * n; e += FFT_THREADS) {
     const int r = e >> llan, l = e & (lanes - 1);
-    if (l < nl) base[r * rs + l] = buf[l * lstride + r];
+    if (l < nl) base[r * rs + l] = buf[l * lstride + fft_pad(r)];
   }
 }
 
@@ -627,7 +635,7 @@ static int poisson_run(Ctx* c, TIO* rhs, cudaStream_t st) {
   {
     const long long nlines = (long long)ny * nz;
     const int lpb = std::max(1, FFT_ELEMS / std::max(M, 1));
-    const size_t smem = (size_t)lpb * M * sizeof(C);
+    const size_t smem = (size_t)lpb * fft_ls(M) * sizeof(C);
     auto k = fft_x_r2c<R, TIO>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const unsigned nb = (unsigned)((nlines + lpb - 1) / lpb);
@@ -635,7 +643,7 @@ static int poisson_run(Ctx* c, TIO* rhs, cudaStream_t st) {
   }
   // B: y forward, lines over kx with stride nxh, outer over z
   const int lanes_y = strided_lanes<C>(ny);
-  const size_t smem_y = (size_t)lanes_y * (ny + 1) * sizeof(C);
+  const size_t smem_y = (size_t)lanes_y * fft_ls(ny) * sizeof(C);
   {
     auto k = fft_strided<R, false, -1>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y);
@@ -645,7 +653,7 @@ static int poisson_run(Ctx* c, TIO* rhs, cudaStream_t st) {
   // C: z forward + Poisson + z inverse; lines over kx, outer over ky
   {
     const int lanes_z = strided_lanes<C>(nz);
-    const size_t smem_z = (size_t)lanes_z * (nz + 1) * sizeof(C);
+    const size_t smem_z = (size_t)lanes_z * fft_ls(nz) * sizeof(C);
     auto k = fft_strided<R, true, -1>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_z);
     dim3 g((nxh + lanes_z - 1) / lanes_z, ny);
@@ -662,7 +670,7 @@ static int poisson_run(Ctx* c, TIO* rhs, cudaStream_t st) {
   {
     const long long nlines = (long long)ny * nz;
     const int lpb = std::max(1, FFT_ELEMS / std::max(M, 1));
-    const size_t smem = (size_t)lpb * M * sizeof(C);
+    const size_t smem = (size_t)lpb * fft_ls(M) * sizeof(C);
     auto k = fft_x_c2r<R, TIO>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const unsigned nb = (unsigned)((nlines + lpb - 1) / lpb);
@@ -849,12 +857,12 @@ int poisson_periodic_noalloc(Ctx* c, double* rhs, cudaStream_t st) {
   sp.scale = 1.0 / ((double)nx * (double)ny * (double)nz);
   const long long nlines = (long long)ny * nz;
   const int lpb = std::max(1, FFT_ELEMS / std::max(M, 1));
-  const size_t smem_x = (size_t)lpb * M * sizeof(C);
+  const size_t smem_x = (size_t)lpb * fft_ls(M) * sizeof(C);
   const unsigned nbx = (unsigned)((nlines + lpb - 1) / lpb);
   const int lanes_y = std::max(1, std::min(32, FFT_ELEMS / ny));
-  const size_t smem_y = (size_t)lanes_y * (ny + 1) * sizeof(C);
+  const size_t smem_y = (size_t)lanes_y * fft_ls(ny) * sizeof(C);
   const int lanes_z = std::max(1, std::min(32, FFT_ELEMS / nz));
-  const size_t smem_z = (size_t)lanes_z * (nz + 1) * sizeof(C);
+  const size_t smem_z = (size_t)lanes_z * fft_ls(nz) * sizeof(C);
   auto kr2c = fft_x_r2c<double>;
   auto kyf = fft_strided<double, false, -1>;
   auto kz = fft_strided<double, true, -1>;
@@ -962,7 +970,7 @@ __device__ void penta_line(double2* e, double* band, int T, int nh, int sys, int
   }
   // inversion5_v1: forward elimination
   const double eps = 1.0e-16;
-  auto E = [&](int m) -> double2& { return e[2 * m + sys]; };
+  auto E = [&](int m) -> double2& { return e[fft_pad(2 * m + sys)]; };
   double tmp = 0.0;
   for (int m = 0; m <= nh - 3; ++m)
     for (int ii = 1; ii <= 2; ++ii) {
@@ -1003,7 +1011,7 @@ __device__ void penta_line(double2* e, double* band, int T, int nh, int sys, int
 __global__ void __launch_bounds__(FFT_THREADS) k_p010_y(double2* __restrict__ data, long long rs, int na, int lanes,
                                                         long long bs, P010 q) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int n = q.nym, nh = n / 2, ls = n + 1;
+  const int n = q.nym, nh = n / 2, ls = fft_ls(n);
   double2* buf = reinterpret_cast<double2*>(smem_raw);
   double* band = reinterpret_cast<double*>(buf + (size_t)lanes * ls);
   const int a0 = blockIdx.x * lanes;
@@ -1014,7 +1022,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_p010_y(double2* __restrict__ da
   for (int e = threadIdx.x; e < lanes * n; e += FFT_THREADS) {
     const int r = e / lanes, l = e - r * lanes;
     const int src = (r < nh) ? 2 * r : 2 * n - 2 * r - 1;
-    if (l < nl) buf[l * ls + r] = base[src * rs + l];
+    if (l < nl) buf[l * ls + fft_pad(r)] = base[src * rs + l];
   }
   __syncthreads();
   smem_fft<-1, double>(buf, ls, n, nl, q.twy_f);
@@ -1022,10 +1030,10 @@ __global__ void __launch_bounds__(FFT_THREADS) k_p010_y(double2* __restrict__ da
   for (int e = threadIdx.x; e < nl * nh; e += FFT_THREADS) {
     const int l = e / nh, j = 1 + (e - l * nh), jp = n - j;
     double2* line = buf + l * ls;
-    const double2 v = line[j], w = line[jp];
+    const double2 v = line[fft_pad(j)], w = line[fft_pad(jp)];
     const double2 sv = make_double2(v.x * q.scale, v.y * q.scale), sw = make_double2(w.x * q.scale, w.y * q.scale);
-    line[j] = cosine_fwd(sv, sw, q.say[j], q.sby[j]);
-    if (jp != j) line[jp] = cosine_fwd(sw, sv, q.say[jp], q.sby[jp]);
+    line[fft_pad(j)] = cosine_fwd(sv, sw, q.say[j], q.sby[j]);
+    if (jp != j) line[fft_pad(jp)] = cosine_fwd(sw, sv, q.say[jp], q.sby[jp]);
     if (j == 1) line[0] = make_double2(line[0].x * q.scale, line[0].y * q.scale);
   }
   __syncthreads();
@@ -1037,7 +1045,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_p010_y(double2* __restrict__ da
                    pxy = __dmul_rn(q.trx[kx], q.ty[j]);
       const double kk = __dadd_rn(__dadd_rn(__dmul_rn(q.kx2[kx], __dmul_rn(pyz, pyz)), __dmul_rn(q.yk2[j], __dmul_rn(pxz, pxz))),
                                   __dmul_rn(q.kz2[kz], __dmul_rn(pxy, pxy)));
-      double2& v = buf[l * ls + j];
+      double2& v = buf[l * ls + fft_pad(j)];
       if (fabs(kk) < 1.0e-16) v = make_double2(0.0, 0.0);
       else v = make_double2(v.x / (-kk), v.y / (-kk));
     }
@@ -1050,22 +1058,22 @@ __global__ void __launch_bounds__(FFT_THREADS) k_p010_y(double2* __restrict__ da
   if (kz == q.nz / 2)
     for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
       const int l = e / n, j = e - l * n;
-      if (a0 + l == q.nx / 2) buf[l * ls + j] = make_double2(0.0, 0.0);
+      if (a0 + l == q.nx / 2) buf[l * ls + fft_pad(j)] = make_double2(0.0, 0.0);
     }
   __syncthreads();
   for (int e = threadIdx.x; e < nl * nh; e += FFT_THREADS) {
     const int l = e / nh, j = 1 + (e - l * nh), jp = n - j;
     double2* line = buf + l * ls;
-    const double2 v = line[j], w = line[jp];
-    line[j] = cosine_bwd(v, w, q.say[j], q.sby[j]);
-    if (jp != j) line[jp] = cosine_bwd(w, v, q.say[jp], q.sby[jp]);
+    const double2 v = line[fft_pad(j)], w = line[fft_pad(jp)];
+    line[fft_pad(j)] = cosine_bwd(v, w, q.say[j], q.sby[j]);
+    if (jp != j) line[fft_pad(jp)] = cosine_bwd(w, v, q.say[jp], q.sby[jp]);
   }
   __syncthreads();
   smem_fft<1, double>(buf, ls, n, nl, q.twy_i);
   for (int e = threadIdx.x; e < lanes * n; e += FFT_THREADS) {
     const int r = e / lanes, l = e - r * lanes;
     const int dst = (r < nh) ? 2 * r : 2 * n - 2 * r - 1;
-    if (l < nl) base[dst * rs + l] = buf[l * ls + r];
+    if (l < nl) base[dst * rs + l] = buf[l * ls + fft_pad(r)];
   }
 }
 
@@ -1150,7 +1158,7 @@ int poisson_010(Ctx* c, double* rhs, cudaStream_t st) {
   // A: x r2c
   const long long nlines = (long long)nym * nz;
   const int lpb = std::max(1, FFT_ELEMS / std::max(M, 1));
-  const size_t smem_x = (size_t)lpb * M * sizeof(C);
+  const size_t smem_x = (size_t)lpb * fft_ls(M) * sizeof(C);
   const unsigned nbx = (unsigned)((nlines + lpb - 1) / lpb);
   {
     auto k = fft_x_r2c<double>;
@@ -1159,7 +1167,7 @@ int poisson_010(Ctx* c, double* rhs, cudaStream_t st) {
   }
   // B: z forward; lines over kx, outer over y
   const int lanes_z = strided_lanes<C>(nz);
-  const size_t smem_z = (size_t)lanes_z * (nz + 1) * sizeof(C);
+  const size_t smem_z = (size_t)lanes_z * fft_ls(nz) * sizeof(C);
   const dim3 gz((nxh + lanes_z - 1) / lanes_z, nym);
   {
     auto k = fft_strided<double, false, -1>;
@@ -1170,7 +1178,7 @@ int poisson_010(Ctx* c, double* rhs, cudaStream_t st) {
   {
     const int nh = nym / 2;
     int lanes = std::max(1, std::min(16, FFT_ELEMS / nym));
-    auto smem_of = [&](int ln) { return (size_t)ln * (nym + 1) * sizeof(C) + (size_t)(2 * ln) * 5 * nh * sizeof(double); };
+    auto smem_of = [&](int ln) { return (size_t)ln * fft_ls(nym) * sizeof(C) + (size_t)(2 * ln) * 5 * nh * sizeof(double); };
     while (lanes > 1 && smem_of(lanes) > 200 * 1024) lanes /= 2;
     const size_t smem = smem_of(lanes);
     q.nsolve = 2 * lanes;
@@ -1239,7 +1247,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_p11(double2* __restrict__ W, do
                                                      int lanes) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = (MODE == P11_X) ? q.NX : (MODE == P11_YF || MODE == P11_YB) ? q.NY : q.NZ;
-  const int ls = n + 1;
+  const int ls = fft_ls(n);
   double2* buf = reinterpret_cast<double2*>(smem_raw);
   double2* bf2 = buf + (size_t)lanes * ls;
   const int NX = q.NX, NY = q.NY, NZ = q.NZ, NZ2 = q.NZ2;
@@ -1261,7 +1269,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_p11(double2* __restrict__ W, do
       if (l < nl) {
         const int i = a0 + l, k = r;
         const int pk = q.bcz ? slip_perm(k, NZ) : k;
-        buf[l * ls + r] = make_double2(rhs[(size_t)slip_perm(i, NX) + (size_t)NX * ((size_t)pj + (size_t)NY * pk)], 0.0);
+        buf[l * ls + fft_pad(r)] = make_double2(rhs[(size_t)slip_perm(i, NX) + (size_t)NX * ((size_t)pj + (size_t)NY * pk)], 0.0);
       }
     }
   } else if (MODE == P11_ZB) {
@@ -1270,7 +1278,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_p11(double2* __restrict__ W, do
       if (l < nl) {
         const double2 v = W[sidx(l, r)];
         // backward z combination (src/poisson.f90:1395-1404)
-        buf[l * ls + r] = make_double2(v.x * q.sbz[r] - v.y * q.saz[r], v.y * q.sbz[r] + v.x * q.saz[r]);
+        buf[l * ls + fft_pad(r)] = make_double2(v.x * q.sbz[r] - v.y * q.saz[r], v.y * q.sbz[r] + v.x * q.saz[r]);
       }
     }
     __syncthreads();
@@ -1279,21 +1287,21 @@ __global__ void __launch_bounds__(FFT_THREADS) k_p11(double2* __restrict__ W, do
       const int l = e / n, r = e - l * n;
       if (l < nl) {
         if (r >= NZ2) {
-          const double2 v = buf[l * ls + (n - r)];
-          buf[l * ls + r] = make_double2(v.x, -v.y);
+          const double2 v = buf[l * ls + fft_pad((n - r))];
+          buf[l * ls + fft_pad(r)] = make_double2(v.x, -v.y);
         }
       }
     }
     __syncthreads();
     for (int l = threadIdx.x; l < nl; l += FFT_THREADS) {
       buf[l * ls].y = 0.0;
-      if ((n & 1) == 0) buf[l * ls + n / 2].y = 0.0;
+      if ((n & 1) == 0) buf[l * ls + fft_pad(n / 2)].y = 0.0;
     }
   } else {
     for (int e = threadIdx.x; e < lanes * n; e += FFT_THREADS) {
       int l, r;
       if (MODE == P11_X) { l = e / n; r = e - l * n; } else { r = e / lanes; l = e - r * lanes; }
-      if (l < nl) buf[l * ls + r] = W[sidx(l, r)];
+      if (l < nl) buf[l * ls + fft_pad(r)] = W[sidx(l, r)];
     }
   }
   __syncthreads();
@@ -1301,12 +1309,12 @@ __global__ void __launch_bounds__(FFT_THREADS) k_p11(double2* __restrict__ W, do
   if (MODE == P11_YB) {
     for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
       const int l = e / n, m = e - l * n;
-      bf2[l * ls + m] = (m == 0) ? buf[l * ls] : p11_bwd(buf[l * ls + m], buf[l * ls + n - m], q.sby[m], q.say[m]);
+      bf2[l * ls + fft_pad(m)] = (m == 0) ? buf[l * ls] : p11_bwd(buf[l * ls + fft_pad(m)], buf[l * ls + fft_pad(n - m)], q.sby[m], q.say[m]);
     }
     __syncthreads();
     for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
       const int l = e / n, m = e - l * n;
-      buf[l * ls + m] = bf2[l * ls + m];
+      buf[l * ls + fft_pad(m)] = bf2[l * ls + fft_pad(m)];
     }
     __syncthreads();
   }
@@ -1319,21 +1327,21 @@ __global__ void __launch_bounds__(FFT_THREADS) k_p11(double2* __restrict__ W, do
   if (MODE == P11_ZF) {
     for (int e = threadIdx.x; e < nl * NZ2; e += FFT_THREADS) {
       const int l = e / NZ2, k = e - l * NZ2;
-      const double2 v = buf[l * ls + k];
+      const double2 v = buf[l * ls + fft_pad(k)];
       // src/poisson.f90:1117-1126
-      buf[l * ls + k] = make_double2(v.x * q.sbz[k] + v.y * q.saz[k], v.y * q.sbz[k] - v.x * q.saz[k]);
+      buf[l * ls + fft_pad(k)] = make_double2(v.x * q.sbz[k] + v.y * q.saz[k], v.y * q.sbz[k] - v.x * q.saz[k]);
     }
     __syncthreads();
   }
   if (MODE == P11_YF) {
     for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
       const int l = e / n, m = e - l * n;
-      bf2[l * ls + m] = (m == 0) ? buf[l * ls] : p11_fwd(buf[l * ls + m], buf[l * ls + n - m], q.sby[m], q.say[m]);
+      bf2[l * ls + fft_pad(m)] = (m == 0) ? buf[l * ls] : p11_fwd(buf[l * ls + fft_pad(m)], buf[l * ls + fft_pad(n - m)], q.sby[m], q.say[m]);
     }
     __syncthreads();
     for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
       const int l = e / n, m = e - l * n;
-      buf[l * ls + m] = bf2[l * ls + m];
+      buf[l * ls + fft_pad(m)] = bf2[l * ls + fft_pad(m)];
     }
     __syncthreads();
   }
@@ -1341,7 +1349,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_p11(double2* __restrict__ W, do
     const int k = b;
     for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
       const int l = e / n, m = e - l * n;
-      double2 v = (m == 0) ? buf[l * ls] : p11_fwd(buf[l * ls + m], buf[l * ls + n - m], q.sbx[m], q.sax[m]);
+      double2 v = (m == 0) ? buf[l * ls] : p11_fwd(buf[l * ls + fft_pad(m)], buf[l * ls + fft_pad(n - m)], q.sbx[m], q.sax[m]);
       // normalisation (src/poisson.f90:1113-1114)
       v = make_double2(v.x / (double)NX / (double)NY / (double)NZ, v.y / (double)NX / (double)NY / (double)NZ);
       // division with the reference's guards (src/poisson.f90:1200-1224)
@@ -1352,12 +1360,12 @@ __global__ void __launch_bounds__(FFT_THREADS) k_p11(double2* __restrict__ W, do
       else if (r0) v = make_double2(0.0, v.y / (-kk.y));
       else if (i0) v = make_double2(v.x / (-kk.x), 0.0);
       else v = make_double2(v.x / (-kk.x), v.y / (-kk.y));
-      bf2[l * ls + m] = v;
+      bf2[l * ls + fft_pad(m)] = v;
     }
     __syncthreads();
     for (int e = threadIdx.x; e < nl * n; e += FFT_THREADS) {
       const int l = e / n, m = e - l * n;
-      buf[l * ls + m] = (m == 0) ? bf2[l * ls] : p11_bwd(bf2[l * ls + m], bf2[l * ls + n - m], q.sbx[m], q.sax[m]);
+      buf[l * ls + fft_pad(m)] = (m == 0) ? bf2[l * ls] : p11_bwd(bf2[l * ls + fft_pad(m)], bf2[l * ls + fft_pad(n - m)], q.sbx[m], q.sax[m]);
     }
     __syncthreads();
     smem_fft<1, double>(buf, ls, n, nl, q.twx_i);
@@ -1370,7 +1378,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_p11(double2* __restrict__ W, do
       if (l < nl) {
         const int i = a0 + l, k = r;
         const int pk = q.bcz ? slip_perm(k, NZ) : k;
-        rhs[(size_t)slip_perm(i, NX) + (size_t)NX * ((size_t)pj + (size_t)NY * pk)] = buf[l * ls + r].x;
+        rhs[(size_t)slip_perm(i, NX) + (size_t)NX * ((size_t)pj + (size_t)NY * pk)] = buf[l * ls + fft_pad(r)].x;
       }
     }
   } else {
@@ -1378,7 +1386,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_p11(double2* __restrict__ W, do
     for (int e = threadIdx.x; e < lanes * rows; e += FFT_THREADS) {
       int l, r;
       if (MODE == P11_X) { l = e / rows; r = e - l * rows; } else { r = e / lanes; l = e - r * lanes; }
-      if (l < nl) W[sidx(l, r)] = buf[l * ls + r];
+      if (l < nl) W[sidx(l, r)] = buf[l * ls + fft_pad(r)];
     }
   }
 }
@@ -1468,7 +1476,7 @@ int poisson_11x(Ctx* c, double* rhs, cudaStream_t st) {
   q.kxyz = reinterpret_cast<const double2*>(s);
   auto launch = [&](auto kern, int n, int na, int nb) -> int {
     const int lanes = std::max(1, std::min(32, FFT_ELEMS / n));
-    const size_t smem = (size_t)2 * lanes * (n + 1) * sizeof(double2);
+    const size_t smem = (size_t)2 * lanes * fft_ls(n) * sizeof(double2);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e);
     const dim3 g((unsigned)((na + lanes - 1) / lanes), (unsigned)nb);
