@@ -81,6 +81,37 @@ __global__ void k_intt_df(Intt3 a, float c1, float c2, float c3, int nh, long lo
   }
 }
 
+// The same update on 4 consecutive points per thread with 16-byte accesses
+// (n a multiple of 4, 16-byte aligned fields): fewer instructions per byte.
+__device__ __forceinline__ float f4get(const float4& v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
+__device__ __forceinline__ void f4set(float4& v, int k, float x) {
+  if (k == 0) v.x = x; else if (k == 1) v.y = x; else if (k == 2) v.z = x; else v.w = x;
+}
+__global__ void k_intt_df4(Intt3 a, float c1, float c2, float c3, int nh, long long n4) {
+  GRID_STRIDE(i, n4) {
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const float4 h0 = reinterpret_cast<const float4*>(a.h[q][0])[i];
+      const float4 h1 = nh > 1 ? reinterpret_cast<const float4*>(a.h[q][1])[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 h2 = nh > 2 ? reinterpret_cast<const float4*>(a.h[q][2])[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 uh = reinterpret_cast<const float4*>(a.uh[q])[i];
+      float4 ul = reinterpret_cast<const float4*>(a.ul[q])[i];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        float inc = c1 * f4get(h0, k);
+        if (nh > 1) inc = inc + c2 * f4get(h1, k);
+        if (nh > 2) inc = inc + c3 * f4get(h2, k);
+        float h = f4get(uh, k), l = f4get(ul, k);
+        df_add_f(h, l, inc);
+        f4set(uh, k, h);
+        f4set(ul, k, l);
+      }
+      reinterpret_cast<float4*>(a.uh[q])[i] = uh;
+      reinterpret_cast<float4*>(a.ul[q])[i] = ul;
+    }
+  }
+}
+
 // cor_vel on the double-float state: u -= grad p (FP32 gradient)
 struct Cor3 {
   float* uh[3];
@@ -95,6 +126,26 @@ __global__ void k_corvel_df(Cor3 a, long long n) {
       df_add_f(h, l, -a.p[q][i]);
       a.uh[q][i] = h;
       a.ul[q][i] = l;
+    }
+  }
+}
+
+__global__ void k_corvel_df4(Cor3 a, long long n4) {
+  GRID_STRIDE(i, n4) {
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const float4 p = reinterpret_cast<const float4*>(a.p[q])[i];
+      float4 uh = reinterpret_cast<const float4*>(a.uh[q])[i];
+      float4 ul = reinterpret_cast<const float4*>(a.ul[q])[i];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        float h = f4get(uh, k), l = f4get(ul, k);
+        df_add_f(h, l, -f4get(p, k));
+        f4set(uh, k, h);
+        f4set(ul, k, l);
+      }
+      reinterpret_cast<float4*>(a.uh[q])[i] = uh;
+      reinterpret_cast<float4*>(a.ul[q])[i] = ul;
     }
   }
 }
@@ -947,7 +998,8 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
       a.ul[q] = s->ul[q];
       for (int k = 0; k < 3; ++k) a.h[q][k] = (const float*)s->H[q][k];
     }
-    k_intt_df<<<nb, 256, 0, st>>>(a, (float)c1, (float)c2, (float)c3, nh, N);
+    if (N % 4 == 0) k_intt_df4<<<nb, 256, 0, st>>>(a, (float)c1, (float)c2, (float)c3, nh, N / 4);
+    else k_intt_df<<<nb, 256, 0, st>>>(a, (float)c1, (float)c2, (float)c3, nh, N);
     s->launches++;
   } else {
     double* U[3] = {s->ux, s->uy, s->uz};
@@ -1010,7 +1062,8 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
       a.ul[q] = s->ul[q];
       a.p[q] = (const float*)w[q];
     }
-    k_corvel_df<<<nb, 256, 0, st>>>(a, N);
+    if (N % 4 == 0) k_corvel_df4<<<nb, 256, 0, st>>>(a, N / 4);
+    else k_corvel_df<<<nb, 256, 0, st>>>(a, N);
   } else {
     k_corvel<T><<<nb, 256, 0, st>>>(s->ux, s->uy, s->uz, w[0], w[1], w[2], N);
   }
