@@ -23,7 +23,8 @@ def _sources():
 
 
 def _deps():
-    return _sources() + glob.glob(os.path.join(CSRC, "*.h")) + [os.path.join(ROOT, "include", "x3d_gpu.h")]
+    return (_sources() + glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
+            [os.path.join(ROOT, "include", "x3d_gpu.h"), os.path.abspath(__file__)])
 
 
 def up_to_date():

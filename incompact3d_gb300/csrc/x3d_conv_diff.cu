@@ -219,23 +219,7 @@ int fill_circ(const OpPlan* p, int L, int max_carries, CircOp& c) {
   if (!p->periodic || p->nin != p->nout) return X3D_ERR_UNSUPPORTED;
   const double al = p->alpha;
   if (!(4.0 * al * al < 1.0)) return X3D_ERR_UNSUPPORTED;  // not diagonally dominant
-  // The plan's Thomas factors (forward t_i -= s_i t_{i-1}, backward
-  // t_i = (t_i - f_i t_{i+1}) w_i) must factor the corner-modified circulant
-  // that the periodic branches pair with the Sherman-Morrison correction:
-  // off-diagonals alpha, diagonal 2, 1, ..., 1, 1 + alpha^2.  Coefficient sets
-  // built for other closures (e.g. the "p" sets of the staggered operators on a
-  // periodic axis) stay on the Thomas kernels.
-  {
-    const int n = p->nout;
-    const double tol = 1e-10;
-    for (int i = 0; i < n; ++i) {
-      const double diag = 1.0 / p->w[i] + (i > 0 ? p->s[i] * p->f[i - 1] : 0.0);
-      const double want = (i == 0) ? 2.0 : (i == n - 1 ? 1.0 + al * al : 1.0);
-      if (std::fabs(diag - want) > tol * want) return X3D_ERR_UNSUPPORTED;
-      if (i < n - 1 && std::fabs(p->f[i] - al) > tol * std::fabs(al) + 1e-300) return X3D_ERR_UNSUPPORTED;
-      if (i > 0 && std::fabs(p->s[i] / p->w[i - 1] - al) > tol * std::fabs(al) + 1e-300) return X3D_ERR_UNSUPPORTED;
-    }
-  }
+  if (!plan_is_circulant(p)) return X3D_ERR_UNSUPPORTED;
   const double mu = 2.0 * al / (1.0 + std::sqrt(1.0 - 4.0 * al * al));
   const double sc = 1.0 + mu * mu;
   std::memset(&c, 0, sizeof(c));

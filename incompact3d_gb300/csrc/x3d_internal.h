@@ -77,6 +77,9 @@ struct Ctx;
 int build_axis(AxisCoef& a, int n, double len, int ncl1, int ncln, const x3d_numopts& o);
 // Build the plan of one operator (host part).  Returns X3D_OK or an error.
 int build_plan(const AxisCoef& a, int axis, int kind, int npaire, int coefset, OpPlan& p);
+// True when a periodic plan's Thomas factors are those of the corner-modified
+// circulant [alpha, 1, alpha] (the solve is then A^-1 b, A circulant).
+bool plan_is_circulant(const OpPlan* p);
 // Default coefficient set for (kind, npaire) as the reference's callers pick it.
 int default_coefset(int kind, int npaire);
 // Index (X3D_COEF_*) of the (f, s, w) vectors of a plan's coefficient set.

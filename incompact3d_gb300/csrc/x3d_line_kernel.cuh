@@ -61,10 +61,20 @@ struct LineArgs {
   const T *s, *f, *w, *pf, *qb, *rsm, *pp;
   T ca, cb, cc, cd, alpha, den;
   int periodic, nterms_int, nbrows;
+  // circulant form of a periodic line (circ = 1): A = (I + mu S)(I + mu S^-1)
+  // / (1 + mu^2) with ca..cd pre-scaled by 1 + mu^2; forward / backward
+  // recurrences with the constant -mu, chunk fix-ups cpw[k] = (-mu)^(k+1) and
+  // cqw[k] = (-mu)^(L-k), cyclic carries from cJ neighbouring chunks with the
+  // multiplier cA = (-mu)^L; no Sherman-Morrison pass
+  int circ, cJ;
+  T cnmu, cA;
+  T cpw[32], cqw[32];
   BRowD<T> brows[kMaxBRows];
   Fuse<T> fz;
 };
 
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
@@ -138,8 +148,8 @@ __device__ __forceinline__ T rhs_row(const LineArgs<T>& p, const T* tile, int la
   return T(0);
 }
 
-template <typename T, int KIND, bool XL, int LMAX>
-__global__ void __launch_bounds__(LANES* CHUNKS) line_kernel(const __grid_constant__ LineArgs<T> p) {
+template <typename T, int KIND, bool XL, int LMAX, bool CIRC>
+__device__ __forceinline__ void line_body(const LineArgs<T>& p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* tile = reinterpret_cast<T*>(smem_raw);
   const int nin = p.nin, nout = p.nout;
@@ -190,6 +200,37 @@ __global__ void __launch_bounds__(LANES* CHUNKS) line_kernel(const __grid_consta
     v[k] = (r < r1) ? rhs_row<T, KIND>(p, tile, lane, r) : T(0);
   }
 
+  if constexpr (CIRC) {
+    // circulant form: every chunk is full (n = CHUNKS * L)
+    T y = T(0);
+#pragma unroll
+    for (int k = 0; k < LMAX; ++k)
+      if (k < L) {
+        y = fma_t(p.cnmu, y, v[k]);
+        v[k] = y;
+      }
+    cfw[ch * LANES + lane] = y;
+    __syncthreads();
+    T cin = T(0);
+    for (int j = p.cJ; j >= 1; --j) cin = fma_t(p.cA, cin, cfw[((ch - j) & (CHUNKS - 1)) * LANES + lane]);
+#pragma unroll
+    for (int k = 0; k < LMAX; ++k)
+      if (k < L) v[k] = fma_t(p.cpw[k], cin, v[k]);
+    T x = T(0);
+#pragma unroll
+    for (int k = LMAX - 1; k >= 0; --k)
+      if (k < L) {
+        x = fma_t(p.cnmu, x, v[k]);
+        v[k] = x;
+      }
+    cbw[ch * LANES + lane] = x;
+    __syncthreads();
+    cin = T(0);
+    for (int j = p.cJ; j >= 1; --j) cin = fma_t(p.cA, cin, cbw[((ch + j) & (CHUNKS - 1)) * LANES + lane]);
+#pragma unroll
+    for (int k = 0; k < LMAX; ++k)
+      if (k < L) v[k] = fma_t(p.cqw[k], cin, v[k]);
+  } else {
   // 3. forward elimination: chunk-local, then carry scan + fix-up
   T y = T(0);
 #pragma unroll
@@ -256,6 +297,8 @@ __global__ void __launch_bounds__(LANES* CHUNKS) line_kernel(const __grid_consta
       if (r < r1) v[k] = v[k] - sx * p.rsm[r];
     }
   }
+  }  // Thomas form
+
   if (p.pp) {
 #pragma unroll
     for (int k = 0; k < LMAX; ++k) {
@@ -293,15 +336,27 @@ __global__ void __launch_bounds__(LANES* CHUNKS) line_kernel(const __grid_consta
   }
 }
 
+// Thomas form: the register count is left to the compiler (64 for the
+// shorter chunks, two blocks per SM).  Circulant form: one block per SM
+// guaranteed, so the long-chunk variant keeps its rows in registers.
+template <typename T, int KIND, bool XL, int LMAX>
+__global__ void __launch_bounds__(LANES* CHUNKS) line_kernel(const __grid_constant__ LineArgs<T> p) {
+  line_body<T, KIND, XL, LMAX, false>(p);
+}
+template <typename T, int KIND, bool XL, int LMAX>
+__global__ void __launch_bounds__(LANES* CHUNKS, 1) line_kernel_circ(const __grid_constant__ LineArgs<T> p) {
+  line_body<T, KIND, XL, LMAX, true>(p);
+}
+
 template <typename T>
 size_t line_smem(int nin, int nout) {
   const int nmax = std::max(nin, nout);
   return sizeof(T) * ((size_t)nmax * LD + 2 * CHUNKS * LANES + 2 * LANES);
 }
 
-template <typename T, int KIND, bool XL, int LMAX>
+template <typename T, int KIND, bool XL, int LMAX, bool CIRC = false>
 int launch_k(const LineArgs<T>& a, dim3 grid, size_t smem, cudaStream_t st) {
-  auto kern = line_kernel<T, KIND, XL, LMAX>;
+  auto kern = CIRC ? line_kernel_circ<T, KIND, XL, LMAX> : line_kernel<T, KIND, XL, LMAX>;
   static size_t configured = 0;  // largest dynamic smem opted in so far (per instantiation)
   if (smem > configured) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -314,6 +369,16 @@ int launch_k(const LineArgs<T>& a, dim3 grid, size_t smem, cudaStream_t st) {
 
 template <typename T, int KIND>
 int dispatch_xl(const LineArgs<T>& a, bool xl, int lmax, dim3 grid, size_t smem, cudaStream_t st) {
+  if (a.circ) {
+    if (xl) {
+      if (lmax == 8) return launch_k<T, KIND, true, 8, true>(a, grid, smem, st);
+      if (lmax == 16) return launch_k<T, KIND, true, 16, true>(a, grid, smem, st);
+      return launch_k<T, KIND, true, 32, true>(a, grid, smem, st);
+    }
+    if (lmax == 8) return launch_k<T, KIND, false, 8, true>(a, grid, smem, st);
+    if (lmax == 16) return launch_k<T, KIND, false, 16, true>(a, grid, smem, st);
+    return launch_k<T, KIND, false, 32, true>(a, grid, smem, st);
+  }
   if (xl) {
     if (lmax == 8) return launch_k<T, KIND, true, 8>(a, grid, smem, st);
     if (lmax == 16) return launch_k<T, KIND, true, 16>(a, grid, smem, st);

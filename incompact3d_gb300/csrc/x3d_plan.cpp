@@ -586,4 +586,27 @@ void kxyz_11x(const AxisCoef& ax, const AxisCoef& ay, const AxisCoef& az, dvec& 
   }
 }
 
+// A periodic plan whose Thomas factors (forward t_i -= s_i t_{i-1}, backward
+// t_i = (t_i - f_i t_{i+1}) w_i) factor the corner-modified circulant that the
+// periodic branches pair with the Sherman-Morrison correction: off-diagonals
+// alpha, diagonal 2, 1, ..., 1, 1 + alpha^2.  Its solve is then A^-1 b with A
+// = I + alpha (S + S^-1) circulant.  Coefficient sets built for other
+// closures (e.g. the "p" sets of the staggered derivative on a periodic axis)
+// are not.
+bool plan_is_circulant(const OpPlan* p) {
+  if (!p->periodic || p->nin != p->nout) return false;
+  const double al = p->alpha;
+  if (!(4.0 * al * al < 1.0)) return false;
+  const int n = p->nout;
+  const double tol = 1e-10;
+  for (int i = 0; i < n; ++i) {
+    const double diag = 1.0 / p->w[i] + (i > 0 ? p->s[i] * p->f[i - 1] : 0.0);
+    const double want = (i == 0) ? 2.0 : (i == n - 1 ? 1.0 + al * al : 1.0);
+    if (std::fabs(diag - want) > tol * want) return false;
+    if (i < n - 1 && std::fabs(p->f[i] - al) > tol * std::fabs(al) + 1e-300) return false;
+    if (i > 0 && std::fabs(p->s[i] / p->w[i - 1] - al) > tol * std::fabs(al) + 1e-300) return false;
+  }
+  return true;
+}
+
 }  // namespace x3d
