@@ -320,6 +320,23 @@ int x3d_solver_destroy(x3d_solver* s);
 /* Copy the velocity in or out.  on_device: 1 = device pointers, 0 = host. */
 int x3d_solver_set_velocity(x3d_solver* s, const double* ux, const double* uy, const double* uz, int on_device);
 int x3d_solver_get_velocity(x3d_solver* s, double* ux, double* uy, double* uz, int on_device);
+/* Asynchronous forms for page-locked host buffers (cudaHostAlloc /
+ * pin_memory; X3D_ERR_ARG otherwise), stream-ordered with x3d_solver_step on
+ * the same stream: set_velocity_async replaces the velocity after the work
+ * already queued on `stream` and before any later step, keeping the time
+ * level and the integrator history (a round trip of the state through host
+ * memory, unlike x3d_solver_set_velocity, which restarts the time
+ * integration); get_velocity_async writes the velocity as of the work queued
+ * on `stream`.  Read-outs run in the order u, v, w on one transfer stream,
+ * write-ins on another, each after its own component's read-out, so in a
+ * set / step / get loop on shared buffers the write-in of one component
+ * overlaps the read-out of the next.  The host buffers are complete after x3d_solver_sync (or
+ * a device synchronisation).  No reference counterpart (the reference keeps
+ * its fields in host memory). */
+int x3d_solver_set_velocity_async(x3d_solver* s, const double* ux, const double* uy, const double* uz,
+                                  void* stream);
+int x3d_solver_get_velocity_async(x3d_solver* s, double* ux, double* uy, double* uz, void* stream);
+int x3d_solver_sync(x3d_solver* s);
 /* Initial condition of init_tgv (src/Case-TGV.f90:25-107), iin=1. */
 int x3d_solver_init_tgv(x3d_solver* s);
 /* Advance nsteps time steps (each with its sub-steps), stream-ordered. */

@@ -117,6 +117,9 @@ def load():
         lib.x3d_solver_destroy.argtypes = [P]
         lib.x3d_solver_set_velocity.argtypes = [P, P, P, P, I]
         lib.x3d_solver_get_velocity.argtypes = [P, P, P, P, I]
+        lib.x3d_solver_set_velocity_async.argtypes = [P, P, P, P, P]
+        lib.x3d_solver_get_velocity_async.argtypes = [P, P, P, P, P]
+        lib.x3d_solver_sync.argtypes = [P]
         lib.x3d_solver_init_tgv.argtypes = [P]
         lib.x3d_solver_step.argtypes = [P, I, P]
         lib.x3d_solver_tgv_stats.argtypes = [P, P, P]

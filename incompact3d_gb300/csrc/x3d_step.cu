@@ -511,7 +511,23 @@ struct SolverImpl {
   double* lw[40] = {nullptr}; // LES work fields
   Mlp* mlp = nullptr;         // learned closure (jles = 10), not owned
   std::vector<void*> allocs;
+  // asynchronous host transfers: a read-out stream (xs[0]) and a write-in
+  // stream (xs[1]); per-component events order a component's write-in after
+  // its read-out, and the steps around them
+  bool xfer_init = false;
+  cudaStream_t xs[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev_set[3] = {nullptr, nullptr, nullptr}, ev_get[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev_step = nullptr;
   ~SolverImpl() {
+    if (xfer_init) {
+      for (int q = 0; q < 3; ++q) {
+        cudaStreamSynchronize(xs[q]);
+        cudaStreamDestroy(xs[q]);
+        cudaEventDestroy(ev_set[q]);
+        cudaEventDestroy(ev_get[q]);
+      }
+      cudaEventDestroy(ev_step);
+    }
     for (void* p : allocs) cudaFree(p);
     if (hpart) cudaFreeHost(hpart);
     if (cf) x3d_ctx_destroy(cf);
@@ -1305,9 +1321,150 @@ __global__ void k_copy64(double* d, const double* s, long long n) {
   GRID_STRIDE(i, n) d[i] = s[i];
 }
 
+// Host <-> device kernels of the asynchronous transfers: 16-byte accesses,
+// four in flight per thread, two blocks per SM, so that the kernels of
+// different components run side by side (one reading host memory while
+// another writes it) instead of each filling the GPU in turn.
+__global__ void __launch_bounds__(256) k_xin(float* uh, float* ul, double* u, const double* h, long long n2) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n2; i0 += 4 * stride) {
+    double2 v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const long long i = i0 + k * stride;
+      if (i < n2) v[k] = reinterpret_cast<const double2*>(h)[i];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const long long i = i0 + k * stride;
+      if (i >= n2) continue;
+      if (u) {
+        reinterpret_cast<double2*>(u)[i] = v[k];
+      } else {
+        const float hx = (float)v[k].x, hy = (float)v[k].y;
+        reinterpret_cast<float2*>(uh)[i] = make_float2(hx, hy);
+        reinterpret_cast<float2*>(ul)[i] = make_float2((float)(v[k].x - (double)hx), (float)(v[k].y - (double)hy));
+      }
+    }
+  }
+}
+__global__ void __launch_bounds__(256) k_xout(double* h, const float* uh, const float* ul, const double* u,
+                                              long long n2) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n2; i0 += 4 * stride) {
+    double2 v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const long long i = i0 + k * stride;
+      if (i >= n2) continue;
+      if (u) {
+        v[k] = reinterpret_cast<const double2*>(u)[i];
+      } else {
+        const float2 a = reinterpret_cast<const float2*>(uh)[i], b = reinterpret_cast<const float2*>(ul)[i];
+        v[k] = make_double2((double)a.x + (double)b.x, (double)a.y + (double)b.y);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const long long i = i0 + k * stride;
+      if (i < n2) reinterpret_cast<double2*>(h)[i] = v[k];
+    }
+  }
+}
+
+static int xfer_setup(SolverImpl* si) {
+  if (si->xfer_init) return X3D_OK;
+  for (int q = 0; q < 3; ++q) {
+    if (cudaStreamCreateWithFlags(&si->xs[q], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&si->ev_set[q], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&si->ev_get[q], cudaEventDisableTiming) != cudaSuccess)
+      return X3D_ERR_CUDA;
+  }
+  if (cudaEventCreateWithFlags(&si->ev_step, cudaEventDisableTiming) != cudaSuccess) return X3D_ERR_CUDA;
+  si->xfer_init = true;
+  return X3D_OK;
+}
+
+// Work on the transfer streams must be finished before a synchronous call
+// touches the state or the host buffers.
+static void xfer_drain(SolverImpl* si) {
+  if (si->xfer_init)
+    for (int q = 0; q < 3; ++q) cudaStreamSynchronize(si->xs[q]);
+}
+
+int x3d_solver_set_velocity_async(x3d_solver* s, const double* ux, const double* uy, const double* uz,
+                                  void* stream) {
+  if (!s || !ux || !uy || !uz) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  const void* m[3] = {mapped_host(ux), mapped_host(uy), mapped_host(uz)};
+  if (!m[0] || !m[1] || !m[2]) return X3D_ERR_ARG;  // page-locked host memory only
+  int rc = xfer_setup(si);
+  if (rc != X3D_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  // write-ins run in order on the second transfer stream, after the work
+  // already queued on the caller's stream (the previous step) and each after
+  // its own component's previous read-out (same host buffer, same state):
+  // write-in of u overlaps the read-out of v, and so on
+  cudaEventRecord(si->ev_step, st);
+  cudaStream_t xw = si->xs[1];
+  cudaStreamWaitEvent(xw, si->ev_step, 0);
+  const bool vec = (si->N % 2 == 0);
+  const unsigned nb = vec ? (unsigned)(2 * si->c->num_sms) : pw_blocks(si->c, si->N);
+  double* U[3] = {si->ux, si->uy, si->uz};
+  for (int q = 0; q < 3; ++q) {
+    cudaStreamWaitEvent(xw, si->ev_get[q], 0);
+    if (vec)
+      k_xin<<<nb, 256, 0, xw>>>(si->mixed() ? si->uh[q] : nullptr, si->mixed() ? si->ul[q] : nullptr,
+                                si->mixed() ? nullptr : U[q], (const double*)m[q], si->N / 2);
+    else if (si->mixed())
+      k_split<<<nb, 256, 0, xw>>>(si->uh[q], si->ul[q], (const double*)m[q], si->N);
+    else
+      k_copy64<<<nb, 256, 0, xw>>>(U[q], (const double*)m[q], si->N);
+    cudaEventRecord(si->ev_set[q], xw);
+  }
+  cudaStreamWaitEvent(st, si->ev_set[2], 0);
+  return cuda_status(cudaGetLastError());
+}
+
+int x3d_solver_get_velocity_async(x3d_solver* s, double* ux, double* uy, double* uz, void* stream) {
+  if (!s || !ux || !uy || !uz) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  void* m[3] = {(void*)mapped_host(ux), (void*)mapped_host(uy), (void*)mapped_host(uz)};
+  if (!m[0] || !m[1] || !m[2]) return X3D_ERR_ARG;
+  int rc = xfer_setup(si);
+  if (rc != X3D_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  // read-outs in order u, v, w on the first transfer stream
+  cudaEventRecord(si->ev_step, st);
+  cudaStream_t xr = si->xs[0];
+  cudaStreamWaitEvent(xr, si->ev_step, 0);
+  const bool vec = (si->N % 2 == 0);
+  const unsigned nb = vec ? (unsigned)(2 * si->c->num_sms) : pw_blocks(si->c, si->N);
+  double* U[3] = {si->ux, si->uy, si->uz};
+  for (int q = 0; q < 3; ++q) {
+    if (vec)
+      k_xout<<<nb, 256, 0, xr>>>((double*)m[q], si->mixed() ? si->uh[q] : nullptr,
+                                 si->mixed() ? si->ul[q] : nullptr, si->mixed() ? nullptr : U[q], si->N / 2);
+    else if (si->mixed())
+      k_combine<<<nb, 256, 0, xr>>>((double*)m[q], si->uh[q], si->ul[q], si->N);
+    else
+      k_copy64<<<nb, 256, 0, xr>>>((double*)m[q], U[q], si->N);
+    cudaEventRecord(si->ev_get[q], xr);
+  }
+  return cuda_status(cudaGetLastError());
+}
+
+int x3d_solver_sync(x3d_solver* s) {
+  if (!s) return X3D_ERR_ARG;
+  SolverImpl* si = &s->impl;
+  xfer_drain(si);
+  return cuda_status(cudaDeviceSynchronize());
+}
+
 int x3d_solver_set_velocity(x3d_solver* s, const double* ux, const double* uy, const double* uz, int on_device) {
   if (!s || !ux || !uy || !uz) return X3D_ERR_ARG;
   SolverImpl* si = &s->impl;
+  xfer_drain(si);
   // Page-locked host buffers are read by the kernels directly (over the
   // host-device link), without a staging copy.
   if (!on_device) {
@@ -1335,6 +1492,7 @@ int x3d_solver_set_velocity(x3d_solver* s, const double* ux, const double* uy, c
 int x3d_solver_get_velocity(x3d_solver* s, double* ux, double* uy, double* uz, int on_device) {
   if (!s || !ux || !uy || !uz) return X3D_ERR_ARG;
   SolverImpl* si = &s->impl;
+  xfer_drain(si);
   if (!on_device) {
     void* m[3] = {(void*)mapped_host(ux), (void*)mapped_host(uy), (void*)mapped_host(uz)};
     if (m[0] && m[1] && m[2]) {
@@ -1390,6 +1548,7 @@ static int state_slot(SolverImpl* si, int which, void** ptr, long long* n, bool*
 int x3d_solver_get_field(x3d_solver* s, int which, double* out, int on_device) {
   if (!s || !out) return X3D_ERR_ARG;
   SolverImpl* si = &s->impl;
+  xfer_drain(si);
   void* p = nullptr;
   long long n = 0;
   bool f32 = false;
@@ -1417,6 +1576,7 @@ int x3d_solver_get_field(x3d_solver* s, int which, double* out, int on_device) {
 int x3d_solver_set_field(x3d_solver* s, int which, const double* in, int on_device) {
   if (!s || !in) return X3D_ERR_ARG;
   SolverImpl* si = &s->impl;
+  xfer_drain(si);
   void* p = nullptr;
   long long n = 0;
   bool f32 = false;
@@ -1470,6 +1630,9 @@ int x3d_solver_step(x3d_solver* s, int nsteps, void* stream) {
   if (!s || nsteps < 0) return X3D_ERR_ARG;
   SolverImpl* si = &s->impl;
   cudaStream_t st = (cudaStream_t)stream;
+  // asynchronous read-outs of the state still in flight finish first
+  if (si->xfer_init)
+    for (int q = 0; q < 3; ++q) cudaStreamWaitEvent(st, si->ev_get[q], 0);
   for (int n = 0; n < nsteps; ++n) {
     for (int itr = 1; itr <= si->nsub; ++itr) {
       const int rc = si->mixed() ? substep<float>(si, itr, st) : substep<double>(si, itr, st);
@@ -1488,6 +1651,7 @@ int x3d_solver_launches_per_step(x3d_solver* s) {
 int x3d_solver_tgv_stats(x3d_solver* s, double* out, void* stream) {
   if (!s || !out) return X3D_ERR_ARG;
   SolverImpl* si = &s->impl;
+  xfer_drain(si);
   Ctx* c = si->c;
   cudaStream_t st = (cudaStream_t)stream;
   const int dims[3] = {c->grid.nx, c->grid.ny, c->grid.nz};
@@ -1547,6 +1711,7 @@ int x3d_solver_tgv_stats(x3d_solver* s, double* out, void* stream) {
 int x3d_solver_divmax(x3d_solver* s, double* out, void* stream) {
   if (!s || !out) return X3D_ERR_ARG;
   SolverImpl* si = &s->impl;
+  xfer_drain(si);
   Ctx* c = si->c;
   cudaStream_t st = (cudaStream_t)stream;
   int rc0 = stage64(si, st);

@@ -102,3 +102,40 @@ def test_pinned_host_transfer_matches_pageable(gpu_lib, precision):
         res.append(out)
     for a, b in zip(*res):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_async_round_trip_matches_device_loop(gpu_lib, precision):
+    """set / step / get through pinned host buffers with the stream-ordered
+    calls, against the device-resident run (time level and history kept).  The
+    FP64 state round-trips exactly: bit for bit.  The mixed solver's
+    double-float state round-trips its binary64 value exactly but is re-split
+    into the canonical hi / lo pair, so its binary32 operand can differ in the
+    last bit: 1e-10 of the largest value after 6 steps."""
+    import ctypes
+    import torch
+    n = 64
+    prec = gpu_lib.PREC_FP64 if precision == "fp64" else gpu_lib.PREC_MIXED
+    ctx = gpu_lib.Context(n, n, n, L, L, L)
+    a = gpu_lib.Solver(ctx, 0.005, 1.0 / 1600.0, itimescheme=3, precision=prec)
+    b = gpu_lib.Solver(ctx, 0.005, 1.0 / 1600.0, itimescheme=3, precision=prec)
+    a.init_tgv()
+    b.init_tgv()
+    host = [torch.empty((n, n, n), dtype=torch.float64, pin_memory=True) for _ in range(3)]
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    lib = b.lib
+    lib.x3d_solver_get_velocity_async(b.h, ptr(host[0]), ptr(host[1]), ptr(host[2]), sp)
+    for _ in range(6):
+        a.step(1)
+        assert lib.x3d_solver_set_velocity_async(b.h, ptr(host[0]), ptr(host[1]), ptr(host[2]), sp) == 0
+        b.step(1)
+        assert lib.x3d_solver_get_velocity_async(b.h, ptr(host[0]), ptr(host[1]), ptr(host[2]), sp) == 0
+    assert lib.x3d_solver_sync(b.h) == 0
+    ref = [torch.from_numpy(v) for v in a.get_velocity()]
+    for h, r in zip(host, ref):
+        if precision == "fp64":
+            assert torch.equal(h, r)
+        else:
+            assert relerr(h.numpy(), r.numpy()) < 1e-10
+    assert a.itime == b.itime == 6
