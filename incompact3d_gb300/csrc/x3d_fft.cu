@@ -29,7 +29,7 @@ namespace x3d {
 
 namespace {
 
-constexpr int FFT_THREADS = 512;
+constexpr int FFT_THREADS = 256;
 constexpr int FFT_VALS = 8;  // complex values held per thread per pass
 constexpr int FFT_ELEMS = FFT_THREADS * FFT_VALS;  // complex values per CTA
 
@@ -276,7 +276,7 @@ int strided_lanes(int n) {
 // ---- Pass A: x real-to-complex --------------------------------------------
 // Lines of nx reals -> nx/2+1 complex.  M = nx/2, packed z[m] = x[2m] + i x[2m+1].
 template <typename P, typename TI = double>
-__global__ void __launch_bounds__(FFT_THREADS) fft_x_r2c(const TI* __restrict__ in,
+__global__ void __launch_bounds__(FFT_THREADS, 4) fft_x_r2c(const TI* __restrict__ in,
                                                          typename Cx<P>::T* __restrict__ out, int nx, long long nlines,
                                                          int lpb, const typename Cx<P>::T* __restrict__ tw_half,
                                                          const typename Cx<P>::T* __restrict__ tw_full) {
@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_x_r2c(const TI* __restrict__ 
 
 // ---- Pass E: x complex-to-real (unnormalised inverse) ----------------------
 template <typename P, typename TO = double>
-__global__ void __launch_bounds__(FFT_THREADS) fft_x_c2r(const typename Cx<P>::T* __restrict__ in,
+__global__ void __launch_bounds__(FFT_THREADS, 4) fft_x_c2r(const typename Cx<P>::T* __restrict__ in,
                                                          TO* __restrict__ out, int nx, long long nlines, int lpb,
                                                          const typename Cx<P>::T* __restrict__ tw_half_inv,
                                                          const typename Cx<P>::T* __restrict__ tw_full) {
@@ -466,7 +466,7 @@ __global__ void k_inv_table(void* out, Spec sp) {
 }
 
 template <typename P, bool POISSON, int SIGN>
-__global__ void __launch_bounds__(FFT_THREADS) fft_strided(typename Cx<P>::T* __restrict__ data, int n, long long rs,
+__global__ void __launch_bounds__(FFT_THREADS, 4) fft_strided(typename Cx<P>::T* __restrict__ data, int n, long long rs,
                                                            int na, int lanes, long long bs,
                                                            const typename Cx<P>::T* __restrict__ tw_f,
                                                            const typename Cx<P>::T* __restrict__ tw_i, Spec sp) {
@@ -1008,7 +1008,7 @@ __device__ void penta_line(double2* e, double* band, int T, int nh, int sys, int
 
 // Pass C.  Lines: kx = blockIdx.x*lanes + l (stride 1), kz = blockIdx.y; the
 // y row stride is rs = nx/2+1, the kz plane stride bs = (nx/2+1)*nym.
-__global__ void __launch_bounds__(FFT_THREADS) k_p010_y(double2* __restrict__ data, long long rs, int na, int lanes,
+__global__ void __launch_bounds__(FFT_THREADS, 4) k_p010_y(double2* __restrict__ data, long long rs, int na, int lanes,
                                                         long long bs, P010 q) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = q.nym, nh = n / 2, ls = fft_ls(n);
@@ -1243,7 +1243,7 @@ enum { P11_ZF = 0, P11_YF = 1, P11_X = 2, P11_YB = 3, P11_ZB = 4 };
 // One kernel per stage; a block holds `lanes` lines of length n in shared
 // memory (buf) plus a second buffer for the mode-pair combination.
 template <int MODE>
-__global__ void __launch_bounds__(FFT_THREADS) k_p11(double2* __restrict__ W, double* __restrict__ rhs, P11 q,
+__global__ void __launch_bounds__(FFT_THREADS, 4) k_p11(double2* __restrict__ W, double* __restrict__ rhs, P11 q,
                                                      int lanes) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = (MODE == P11_X) ? q.NX : (MODE == P11_YF || MODE == P11_YB) ? q.NY : q.NZ;
