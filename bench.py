@@ -47,6 +47,23 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(torch, secs, device):
+    """The job's time: the slowest rank's (all-reduce MAX over the process
+    group; the value itself on one process)."""
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return secs
+    t = torch.tensor([float(secs)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(points_per_rank, steps, ws, secs):
+    """Whole-job Mpts*steps/s: the grid points all replicas advanced, over the
+    slowest rank's time (weak scaling: every rank runs the full workload)."""
+    return points_per_rank * steps * ws / secs / 1e6
+
+
 class Clocks:
     """Samples nvidia-smi during the timed region."""
 
@@ -203,10 +220,7 @@ def run_ours(args):
             torch.distributed.barrier()
         with Clocks(local) as clk:
             secs = time_steps(torch, s, args.steps, stream)
-        if ws > 1:
-            t = torch.tensor([secs], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            secs = t.item()
+        secs = max_over_ranks(torch, secs, "cuda")
         res[prec] = {"secs": secs, "clocks": clk.summary(), "launches": launches0}
         solvers[prec] = s
     # kinetic energy of both solvers after the same number of steps
@@ -216,7 +230,7 @@ def run_ours(args):
     if args.no_e2e:
         if rank == 0:
             main = res.get("mixed") or res[list(res)[0]]
-            print(json.dumps({"metric": METRIC, "value": round(N * args.steps * ws / main["secs"] / 1e6, 3),
+            print(json.dumps({"metric": METRIC, "value": round(job_rate(N, args.steps, ws, main["secs"]), 3),
                               "unit": UNIT, "steps": args.steps, "warmup": args.warmup,
                               "ms_per_step": round(1e3 * main["secs"] / args.steps, 3), "partial": "no e2e"}))
         return
@@ -266,7 +280,7 @@ def run_ours(args):
         return
     main = res.get("mixed") or res[list(res)[0]]
     secs = main["secs"]
-    value = N * args.steps * ws / secs / 1e6
+    value = job_rate(N, args.steps, ws, secs)
     cpu_rate, cpu_threads, _ = cpu_oracle_rate(args.cpu_n, 1) if not args.no_cpu else (None, 0, 0)
     achieved = kbytes / ksec / 1e9
     line = {
