@@ -12,6 +12,7 @@ with the kinetic-energy difference between the two after the same steps.
   python bench.py --workload channel [--steps K] [--warmup W]
   python bench.py --workload les [--steps K] [--warmup W]
   python bench.py --workload les_mlp [--n 512] [--t-end 20] [--out results.json]
+  python bench.py --workload freeslip [--steps K] [--warmup W]
 
 --impl reference times the CPU restatement of the reference's path (the
 parity oracle, C++/OpenMP on all host cores) on a bounded sample grid of the
@@ -508,6 +509,36 @@ def run_les(args):
     print(json.dumps(out), flush=True)
 
 
+def run_freeslip(args):
+    """The reference's own regression case (tests/TGV-Taylor-Green-vortex):
+    TGV in the free-slip box [0, pi]^3 with 65^3 nodes, Re = 1600, RK3,
+    dt = 0.005, FP64 (poisson_11x); the statistics row after the timed steps
+    is printed beside the rate for a diff against reference_time_evol.dat."""
+    import numpy as np
+    import torch
+    import incompact3d_gb300 as x3d
+
+    x3d.build()
+    n, L, dt = 65, np.pi, 0.005
+    ctx = x3d.Context(n, n, n, L, L, L, bc=((1, 1), (1, 1), (1, 1)))
+    s = x3d.Solver(ctx, dt, 1 / 1600.0, itimescheme=5, precision=x3d.PREC_FP64)
+    x = np.arange(n) * (L / (n - 1))
+    X, Y, Z = x[None, None, :], x[None, :, None], x[:, None, None]
+    s.set_velocity(np.sin(X) * np.cos(Y) * np.cos(Z), -np.cos(X) * np.sin(Y) * np.cos(Z), np.zeros((n, n, n)))
+    stream = torch.cuda.current_stream()
+    s.step(args.warmup)
+    secs = time_steps(torch, s, args.steps, stream)
+    itime = args.warmup + args.steps
+    st = s.tgv_stats()
+    out = {"workload": "tgv_freeslip_65^3_rk3_fp64", "metric": "free-slip TGV Mpts*steps/s", "unit": UNIT,
+           "value": round(n ** 3 * args.steps / secs / 1e6, 3), "ms_per_step": round(1e3 * secs / args.steps, 3),
+           "steps": args.steps, "warmup": args.warmup, "dtype": "f64",
+           "launches_per_step": s.lib.x3d_solver_launches_per_step(s.h),
+           "stats_row": [(itime - 1) * dt] + [float(v) for v in st]}
+    s.close()
+    print(json.dumps(out), flush=True)
+
+
 def run_les_mlp(args):
     """Learned SGS closure pipeline: TGV DNS at Re=5000 (n^3, mixed solver,
     dt = 0.001; dt = 0.002 diverged near t = 7.3 at 512^3 with AB3) ->
@@ -539,7 +570,7 @@ def run_les_mlp(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "ops", "channel", "les", "les_mlp"],
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "ops", "channel", "les", "les_mlp", "freeslip"],
                     help="tgv: the time-step benchmark (default); ops: operator microbench lines; "
                          "channel: the stretched turbulent channel (FP64)")
     ap.add_argument("--ops", default="", help="ops workload: comma list (derx,...,filz,poisson)")
@@ -571,6 +602,8 @@ def main():
         run_ops(args)
     elif args.workload == "channel":
         run_channel(args)
+    elif args.workload == "freeslip":
+        run_freeslip(args)
     elif args.workload == "les":
         run_les(args)
     elif args.workload == "les_mlp":
