@@ -5,7 +5,7 @@ width to the 6 subgrid stresses tau_ij; it is trained on box-filtered (ratio
 4) snapshots of a DNS run by this package's own solver and then used inside
 the LES time step (``Solver.set_les_mlp``).  The dynamic Smagorinsky model of
 the reference (src/les_models.f90:333-903) is the fallback and the cost
-baseline, and the box-filtered DNS is the judge of the model's error.
+baseline, and the model's error is measured against the box-filtered DNS.
 
 All compute runs in libx3dgpu's kernels (solver, box filter, MLP training and
 inference); PyTorch only holds device buffers and shuffles sample indices.
