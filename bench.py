@@ -504,8 +504,41 @@ def run_les(args):
                      "value": round(n ** 3 * args.steps / secs / 1e6, 3),
                      "launches_per_step": s.lib.x3d_solver_launches_per_step(s.h)}
         s.close()
+    # the learned closure (untrained weights: the cost does not depend on them),
+    # inference on FP32 CUDA cores and on the tensor cores (tcgen05, BF16 split)
+    from incompact3d_gb300 import sgs
+    m = sgs.Mlp(seed=0)
+    for name, tc in (("mlp", False), ("mlp_tc", True)):
+        m.set_tensor_cores(tc)
+        s = x3d.Solver(ctx, 0.005, 1 / 5000.0, itimescheme=3, precision=x3d.PREC_FP64)
+        s.init_tgv()
+        x3d._lib.check(s.lib.x3d_solver_set_les_mlp(s.h, m.h), "x3d_solver_set_les_mlp")
+        s.step(args.warmup)
+        secs = time_steps(torch, s, args.steps, stream)
+        out[name] = {"ms_per_step": round(1e3 * secs / args.steps, 3),
+                     "value": round(n ** 3 * args.steps / secs / 1e6, 3),
+                     "launches_per_step": s.lib.x3d_solver_launches_per_step(s.h)}
+        s.close()
+    X = torch.randn((n ** 3, 10), dtype=torch.float32, device="cuda")
+    flop = 2.0 * n ** 3 * (10 * 64 + 64 * 64 + 64 * 6)
+    for name, tc in (("infer_fp32", False), ("infer_tc", True)):
+        m.set_tensor_cores(tc)
+        for _ in range(3):
+            m.infer(X)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(20):
+            m.infer(X)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 20
+        out[name] = {"points": n ** 3, "ms": round(ms, 4), "tflops_network": round(flop / ms / 1e9, 2)}
+    m.status()
+    m.close()
     out["value"] = out["dynsmag"]["value"]
     out["dynsmag_over_plain"] = round(out["dynsmag"]["ms_per_step"] / out["plain"]["ms_per_step"], 3)
+    out["mlp_tc_over_dynsmag"] = round(out["mlp_tc"]["ms_per_step"] / out["dynsmag"]["ms_per_step"], 3)
     print(json.dumps(out), flush=True)
 
 

@@ -398,6 +398,16 @@ int x3d_mlp_infer(x3d_mlp* m, const float* X, float* Y, long long n, void* strea
  * NULL, synchronises) receives the loss before the step. */
 int x3d_mlp_train_step(x3d_mlp* m, const float* X, const float* T, long long n, float lr, float* loss,
                        void* stream);
+/* Inference on the tensor cores (on = 1; default 0 = FP32 CUDA cores): the
+ * three layers as tcgen05 MMAs of 128 points, BF16 hi / lo split operands
+ * (hi*hi + hi*lo + lo*hi) accumulated in FP32 in tensor memory, within about
+ * 1e-4 relative of the FP32 kernel.  Applies to x3d_mlp_infer and to the
+ * solver's closure (x3d_solver_set_les_mlp). */
+int x3d_mlp_set_tensor_cores(x3d_mlp* m, int on);
+/* X3D_ERR_CUDA if a bounded wait inside a tensor-core inference ran out (the
+ * kernel then stops and leaves its outputs incomplete), else X3D_OK.
+ * Synchronises. */
+int x3d_mlp_status(x3d_mlp* m);
 /* Add lam * ((Pi_model - Pi_target) / pscale)^2 to the training loss, with the
  * subgrid energy flux Pi = tau_ij S_ij (S from the raw gradient features);
  * lam = 0 (default) is the plain stress loss. */

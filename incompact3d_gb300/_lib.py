@@ -139,6 +139,8 @@ def load():
         lib.x3d_mlp_train_step.argtypes = [P, P, P, LL, ctypes.c_float, P, P]
         lib.x3d_box_filter4.argtypes = [P, P, P, I, I, I, P, P, P, P, P]
         lib.x3d_mlp_set_flux_loss.argtypes = [P, ctypes.c_float, ctypes.c_float]
+        lib.x3d_mlp_set_tensor_cores.argtypes = [P, I]
+        lib.x3d_mlp_status.argtypes = [P]
         lib.x3d_solver_set_les_mlp.argtypes = [P, P]
         lib.x3d_solver_set_field.argtypes = [P, I, P, I]
         lib.x3d_solver_get_itime.argtypes = [P]

@@ -163,6 +163,31 @@ struct Mlp;
 int mlp_les_tau(Mlp* m, const double* const* g9, double delta, double* const* tau6, long long n, int num_sms,
                 cudaStream_t st);
 
+// Shape of the closure and offsets of its parameter array:
+// W1[64][10], b1[64], W2[64][64], b2[64], W3[6][64], b3[6].
+namespace mlpdim {
+constexpr int NI = 10, NH = 64, NO = 6;
+constexpr int OW1 = 0;
+constexpr int OB1 = OW1 + NH * NI;
+constexpr int OW2 = OB1 + NH;
+constexpr int OB2 = OW2 + NH * NH;
+constexpr int OW3 = OB2 + NH;
+constexpr int OB3 = OW3 + NO * NH;
+constexpr int NPAR = OB3 + NO;  // 5254
+}  // namespace mlpdim
+
+// Tensor-core (tcgen05) inference of the closure (x3d_mlp_tc.cu).  The weights
+// are packed once per parameter change into the BF16 hi / lo image the MMAs
+// read (MLP_TC_WP_BYTES, 16-byte aligned); err (device int) is set to 1 when a
+// bounded wait on the tensor core or the weight copy runs out.  Features come
+// from X[n][10] (FP32 rows) when X is non-null, else from the 9 gradient
+// fields g9 and delta; results go to Y[n][6] or to tau6.
+constexpr int MLP_TC_WP_BYTES = 24576;
+int mlp_tc_pack(const float* P, void* wp, cudaStream_t st);
+int mlp_tc_infer(const float* P, const float* sc, const void* wp, int* err, const float* X, float* Y,
+                 const double* const* g9, float delta, double* const* tau6, long long n, int num_sms,
+                 cudaStream_t st);
+
 // Device copies of a plan's vectors (made on first use).
 int upload_plan(OpPlan* p);
 // Fused momentum right-hand side along one axis, binary32 periodic lines in

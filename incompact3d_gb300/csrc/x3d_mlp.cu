@@ -19,14 +19,16 @@
 namespace x3d {
 namespace {
 
-constexpr int NI = 10, NH = 64, NO = 6;
-constexpr int OW1 = 0;
-constexpr int OB1 = OW1 + NH * NI;
-constexpr int OW2 = OB1 + NH;
-constexpr int OB2 = OW2 + NH * NH;
-constexpr int OW3 = OB2 + NH;
-constexpr int OB3 = OW3 + NO * NH;
-constexpr int NPAR = OB3 + NO;  // 5254
+using mlpdim::NI;
+using mlpdim::NH;
+using mlpdim::NO;
+using mlpdim::OW1;
+using mlpdim::OB1;
+using mlpdim::OW2;
+using mlpdim::OB2;
+using mlpdim::OW3;
+using mlpdim::OB3;
+using mlpdim::NPAR;
 
 #define GSTRIDE(i, n) \
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (n); i += (long long)gridDim.x * blockDim.x)
@@ -305,14 +307,44 @@ struct Mlp {
   int nbmax = 0;
   int step = 0;
   float lam = 0.f, pscale = 1.f;  // energy-flux loss term
+  // tensor-core inference (x3d_mlp_tc.cu): packed BF16 weight image, rebuilt
+  // after every parameter change, and the device flag of its bounded waits
+  bool tc = false;
+  bool wp_dirty = true;
+  void* wp = nullptr;
+  int* tc_err = nullptr;
   ~Mlp() {
     for (float* p : {P, m1, m2, sc, part, lpart, lsum})
       if (p) cudaFree(p);
+    if (wp) cudaFree(wp);
+    if (tc_err) cudaFree(tc_err);
   }
 };
 
+// Packed weights for the tensor-core kernel, made on first use and after each
+// parameter change (stream-ordered with the update that changed them).
+static int tc_ready(Mlp* m, cudaStream_t st) {
+  if (!m->wp) {
+    if (cudaMalloc(&m->wp, MLP_TC_WP_BYTES) != cudaSuccess) return X3D_ERR_NOMEM;
+    if (cudaMalloc(&m->tc_err, sizeof(int)) != cudaSuccess) return X3D_ERR_NOMEM;
+    if (cudaMemsetAsync(m->tc_err, 0, sizeof(int), st) != cudaSuccess) return X3D_ERR_CUDA;
+    m->wp_dirty = true;
+  }
+  if (m->wp_dirty) {
+    const int rc = mlp_tc_pack(m->P, m->wp, st);
+    if (rc != X3D_OK) return rc;
+    m->wp_dirty = false;
+  }
+  return X3D_OK;
+}
+
 int mlp_les_tau(Mlp* m, const double* const* g9, double delta, double* const* tau6, long long n, int num_sms,
                 cudaStream_t st) {
+  if (m->tc) {
+    const int rc = tc_ready(m, st);
+    if (rc != X3D_OK) return rc;
+    return mlp_tc_infer(m->P, m->sc, m->wp, m->tc_err, nullptr, nullptr, g9, (float)delta, tau6, n, num_sms, st);
+  }
   G9 g;
   T6 t;
   for (int i = 0; i < 9; ++i) g.g[i] = g9[i];
@@ -366,6 +398,7 @@ int x3d_mlp_set_params(x3d_mlp* h, const float* params, const float* scales) {
   if (scales && cudaMemcpy(m->sc, scales, (NI + NO) * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
     return X3D_ERR_CUDA;
   m->step = 0;
+  m->wp_dirty = true;
   cudaMemset(m->m1, 0, NPAR * sizeof(float));
   cudaMemset(m->m2, 0, NPAR * sizeof(float));
   return cuda_status(cudaGetLastError());
@@ -387,6 +420,11 @@ int x3d_mlp_infer(x3d_mlp* h, const float* X, float* Y, long long n, void* strea
   int dev = 0, sms = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (m->tc) {
+    const int rc = tc_ready(m, (cudaStream_t)stream);
+    if (rc != X3D_OK) return rc;
+    return mlp_tc_infer(m->P, m->sc, m->wp, m->tc_err, X, Y, nullptr, 0.f, nullptr, n, sms, (cudaStream_t)stream);
+  }
   const size_t smem = (NPAR + NI + NO) * sizeof(float);
   k_mlp_infer<<<sms * 4, 256, smem, (cudaStream_t)stream>>>(m->P, m->sc, X, Y, n);
   return cuda_status(cudaGetLastError());
@@ -420,6 +458,7 @@ int x3d_mlp_train_step(x3d_mlp* h, const float* X, const float* T, long long n, 
   m->step += 1;
   const float b1c = 1.f - powf(0.9f, (float)m->step), b2c = 1.f - powf(0.999f, (float)m->step);
   k_mlp_adam<<<(NPAR + 255) / 256, 256, 0, st>>>(m->P, m->m1, m->m2, m->part, nb, lr, b1c, b2c);
+  m->wp_dirty = true;
   if (loss) {
     k_sum<<<1, 1, 0, st>>>(m->lpart, nb, m->lsum);
     float hl = 0.f;
@@ -428,6 +467,22 @@ int x3d_mlp_train_step(x3d_mlp* h, const float* X, const float* T, long long n, 
     *loss = hl / (float)n;
   }
   return cuda_status(cudaGetLastError());
+}
+
+int x3d_mlp_set_tensor_cores(x3d_mlp* h, int on) {
+  if (!h || (on != 0 && on != 1)) return X3D_ERR_ARG;
+  Mlp* m = reinterpret_cast<Mlp*>(h);
+  m->tc = on != 0;
+  return X3D_OK;
+}
+
+int x3d_mlp_status(x3d_mlp* h) {
+  if (!h) return X3D_ERR_ARG;
+  Mlp* m = reinterpret_cast<Mlp*>(h);
+  if (!m->tc_err) return X3D_OK;
+  int e = 0;
+  if (cudaMemcpy(&e, m->tc_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return X3D_ERR_CUDA;
+  return e ? X3D_ERR_CUDA : X3D_OK;
 }
 
 int x3d_mlp_set_flux_loss(x3d_mlp* h, float lam, float pscale) {

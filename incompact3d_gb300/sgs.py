@@ -69,6 +69,15 @@ class Mlp:
         check(self.lib.x3d_mlp_set_flux_loss(self.h, ctypes.c_float(lam), ctypes.c_float(pscale)),
               "x3d_mlp_set_flux_loss")
 
+    def set_tensor_cores(self, on=True):
+        """Run inference (x3d_mlp_infer and the solver's closure) as tcgen05
+        MMAs with BF16 hi / lo split operands instead of FP32 CUDA cores."""
+        check(self.lib.x3d_mlp_set_tensor_cores(self.h, 1 if on else 0), "x3d_mlp_set_tensor_cores")
+
+    def status(self):
+        """Raises if a bounded wait inside a tensor-core inference ran out."""
+        check(self.lib.x3d_mlp_status(self.h), "x3d_mlp_status")
+
     def infer(self, X):
         torch = _torch()
         Y = torch.empty((X.shape[0], NOUT), dtype=torch.float32, device=X.device)
