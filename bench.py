@@ -13,6 +13,7 @@ with the kinetic-energy difference between the two after the same steps.
   python bench.py --workload les [--steps K] [--warmup W]
   python bench.py --workload les_mlp [--n 512] [--t-end 20] [--out results.json]
   python bench.py --workload freeslip [--steps K] [--warmup W]
+  python bench.py --workload mlp [--reps R]
 
 --impl reference times the CPU restatement of the reference's path (the
 parity oracle, C++/OpenMP on all host cores) on a bounded sample grid of the
@@ -519,8 +520,22 @@ def run_les(args):
                      "value": round(n ** 3 * args.steps / secs / 1e6, 3),
                      "launches_per_step": s.lib.x3d_solver_launches_per_step(s.h)}
         s.close()
-    X = torch.randn((n ** 3, 10), dtype=torch.float32, device="cuda")
-    flop = 2.0 * n ** 3 * (10 * 64 + 64 * 64 + 64 * 6)
+    out.update(mlp_infer_times(torch, m, n ** 3, 20))
+    m.close()
+    out["value"] = out["dynsmag"]["value"]
+    out["dynsmag_over_plain"] = round(out["dynsmag"]["ms_per_step"] / out["plain"]["ms_per_step"], 3)
+    out["mlp_tc_over_dynsmag"] = round(out["mlp_tc"]["ms_per_step"] / out["dynsmag"]["ms_per_step"], 3)
+    print(json.dumps(out), flush=True)
+
+
+def mlp_infer_times(torch, m, npts, reps):
+    """CUDA-event time of the closure's inference on npts feature rows, FP32
+    CUDA-core kernel and tensor-core kernel; network flops = 2 (10*64 + 64*64
+    + 64*6) per point (the tensor-core kernel issues 3x that as split MMAs)."""
+    stream = torch.cuda.current_stream()
+    X = torch.randn((npts, 10), dtype=torch.float32, device="cuda")
+    flop = 2.0 * npts * (10 * 64 + 64 * 64 + 64 * 6)
+    out = {}
     for name, tc in (("infer_fp32", False), ("infer_tc", True)):
         m.set_tensor_cores(tc)
         for _ in range(3):
@@ -528,17 +543,27 @@ def run_les(args):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record(stream)
-        for _ in range(20):
+        for _ in range(reps):
             m.infer(X)
         e1.record(stream)
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / 20
-        out[name] = {"points": n ** 3, "ms": round(ms, 4), "tflops_network": round(flop / ms / 1e9, 2)}
+        ms = e0.elapsed_time(e1) / reps
+        out[name] = {"points": npts, "ms": round(ms, 4), "tflops_network": round(flop / ms / 1e9, 2)}
     m.status()
+    return out
+
+
+def run_mlp(args):
+    """Inference of the learned closure alone on 128^3 feature rows."""
+    import torch
+    import incompact3d_gb300 as x3d
+    from incompact3d_gb300 import sgs
+
+    x3d.build()
+    m = sgs.Mlp(seed=0)
+    out = {"workload": "sgs_mlp_inference_128^3", "unit": "ms"}
+    out.update(mlp_infer_times(torch, m, 128 ** 3, args.reps))
     m.close()
-    out["value"] = out["dynsmag"]["value"]
-    out["dynsmag_over_plain"] = round(out["dynsmag"]["ms_per_step"] / out["plain"]["ms_per_step"], 3)
-    out["mlp_tc_over_dynsmag"] = round(out["mlp_tc"]["ms_per_step"] / out["dynsmag"]["ms_per_step"], 3)
     print(json.dumps(out), flush=True)
 
 
@@ -603,7 +628,7 @@ def run_les_mlp(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "ops", "channel", "les", "les_mlp", "freeslip"],
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "ops", "channel", "les", "les_mlp", "freeslip", "mlp"],
                     help="tgv: the time-step benchmark (default); ops: operator microbench lines; "
                          "channel: the stretched turbulent channel (FP64)")
     ap.add_argument("--ops", default="", help="ops workload: comma list (derx,...,filz,poisson)")
@@ -637,6 +662,8 @@ def main():
         run_channel(args)
     elif args.workload == "freeslip":
         run_freeslip(args)
+    elif args.workload == "mlp":
+        run_mlp(args)
     elif args.workload == "les":
         run_les(args)
     elif args.workload == "les_mlp":

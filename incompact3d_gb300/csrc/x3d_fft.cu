@@ -69,6 +69,33 @@ __device__ __forceinline__ df df_add(df a, df b) {
 }
 __device__ __forceinline__ df df_neg(df a) { return df{-a.h, -a.l}; }
 __device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
+// Sum without the final renormalisation: hi is the rounded sum of the hi
+// parts, lo collects their exact rounding error and the lo parts.  Used for
+// the inner levels of a butterfly only (at most three in a row, the third
+// feeding a product), whose last level renormalises: the error stays a few
+// 2^-48 of the operands' size.
+__device__ __forceinline__ df df_add_l(df a, df b) {
+  const df s = two_sum(a.h, b.h);
+  return df{s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l))};
+}
+__device__ __forceinline__ df df_sub_l(df a, df b) { return df_add_l(a, df_neg(b)); }
+// x.h*y.h + u.h*v.h (sg = +1) or x.h*y.h - u.h*v.h (sg = -1) with the exact
+// product errors and the cross terms folded into one lo sum, then one
+// renormalisation: the real or imaginary part of a complex product.
+template <int SG>
+__device__ __forceinline__ df df_dot2(df x, df y, df u, df v) {
+  const float p1 = __fmul_rn(x.h, y.h);
+  const float p2 = __fmul_rn(SG > 0 ? u.h : -u.h, v.h);
+  const float e1 = __fmaf_rn(x.h, y.h, -p1);
+  const float e2 = __fmaf_rn(SG > 0 ? u.h : -u.h, v.h, -p2);
+  const df s = two_sum(p1, p2);
+  float t = __fadd_rn(s.l, __fadd_rn(e1, e2));
+  t = __fmaf_rn(x.h, y.l, t);
+  t = __fmaf_rn(x.l, y.h, t);
+  t = __fmaf_rn(SG > 0 ? u.h : -u.h, v.l, t);
+  t = __fmaf_rn(SG > 0 ? u.l : -u.l, v.h, t);
+  return fast_two_sum(s.h, t);
+}
 __device__ __forceinline__ df df_mul(df a, df b) {
   const float p = __fmul_rn(a.h, b.h);
   float e = __fmaf_rn(a.h, b.h, -p);
@@ -98,6 +125,8 @@ struct FTnative {
   typedef typename std::conditional<std::is_same<R, double>::value, double2, float2>::type C;
   static __device__ __forceinline__ C add(C a, C b) { return C{a.x + b.x, a.y + b.y}; }
   static __device__ __forceinline__ C sub(C a, C b) { return C{a.x - b.x, a.y - b.y}; }
+  static __device__ __forceinline__ C add_l(C a, C b) { return add(a, b); }
+  static __device__ __forceinline__ C sub_l(C a, C b) { return sub(a, b); }
   static __device__ __forceinline__ C mul(C a, C b) { return C{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
   static __device__ __forceinline__ C conj(C a) { return C{a.x, -a.y}; }
   static __device__ __forceinline__ C half(C a) { return C{a.x * (R)0.5, a.y * (R)0.5}; }
@@ -136,8 +165,10 @@ struct FT<DF> {
   static __device__ __forceinline__ C mk(df r, df i) { return C{r.h, r.l, i.h, i.l}; }
   static __device__ __forceinline__ C add(C a, C b) { return mk(df_add(R_(a), R_(b)), df_add(I_(a), I_(b))); }
   static __device__ __forceinline__ C sub(C a, C b) { return mk(df_sub(R_(a), R_(b)), df_sub(I_(a), I_(b))); }
+  static __device__ __forceinline__ C add_l(C a, C b) { return mk(df_add_l(R_(a), R_(b)), df_add_l(I_(a), I_(b))); }
+  static __device__ __forceinline__ C sub_l(C a, C b) { return mk(df_sub_l(R_(a), R_(b)), df_sub_l(I_(a), I_(b))); }
   static __device__ __forceinline__ C mul(C a, C b) {
-    return mk(df_sub(df_mul(R_(a), R_(b)), df_mul(I_(a), I_(b))), df_add(df_mul(R_(a), I_(b)), df_mul(I_(a), R_(b))));
+    return mk(df_dot2<-1>(R_(a), R_(b), I_(a), I_(b)), df_dot2<1>(R_(a), I_(b), I_(a), R_(b)));
   }
   static __device__ __forceinline__ C conj(C a) { return C{a.rh, a.rl, -a.ih, -a.il}; }
   static __device__ __forceinline__ C half(C a) { return mk(df_half(R_(a)), df_half(I_(a))); }
@@ -149,14 +180,14 @@ struct FT<DF> {
   template <int S>
   static __device__ __forceinline__ C w8_1(C o) {
     const df x = R_(o), y = I_(o), h = h_();
-    return S < 0 ? mk(df_mul(df_add(x, y), h), df_mul(df_sub(y, x), h))
-                 : mk(df_mul(df_sub(x, y), h), df_mul(df_add(y, x), h));
+    return S < 0 ? mk(df_mul(df_add_l(x, y), h), df_mul(df_sub_l(y, x), h))
+                 : mk(df_mul(df_sub_l(x, y), h), df_mul(df_add_l(y, x), h));
   }
   template <int S>
   static __device__ __forceinline__ C w8_3(C o) {
     const df x = R_(o), y = I_(o), h = h_();
-    return S < 0 ? mk(df_mul(df_sub(y, x), h), df_neg(df_mul(df_add(x, y), h)))
-                 : mk(df_neg(df_mul(df_add(x, y), h)), df_mul(df_sub(x, y), h));
+    return S < 0 ? mk(df_mul(df_sub_l(y, x), h), df_neg(df_mul(df_add_l(x, y), h)))
+                 : mk(df_neg(df_mul(df_add_l(x, y), h)), df_mul(df_sub_l(x, y), h));
   }
   static __device__ __forceinline__ C from(double re, double im) { return mk(df_from(re), df_from(im)); }
   // binary32 values are exact hi parts: no binary64 arithmetic on the way in
@@ -181,15 +212,24 @@ __device__ __forceinline__ void fft2(C& a, C& b) {
   b = FT<P>::sub(t, b);
 }
 
-template <int SIGN, typename P, typename C>
+// INNER: the outputs feed further butterfly levels (inside fft8) and are left
+// unnormalised in double-float arithmetic; else the last level renormalises.
+template <int SIGN, typename P, bool INNER = false, typename C>
 __device__ __forceinline__ void fft4(C& x0, C& x1, C& x2, C& x3) {
   typedef FT<P> F;
-  C s02 = F::add(x0, x2), d02 = F::sub(x0, x2);
-  C s13 = F::add(x1, x3), d13 = F::template mul_i<SIGN>(F::sub(x1, x3));
-  x0 = F::add(s02, s13);
-  x2 = F::sub(s02, s13);
-  x1 = F::add(d02, d13);
-  x3 = F::sub(d02, d13);
+  C s02 = F::add_l(x0, x2), d02 = F::sub_l(x0, x2);
+  C s13 = F::add_l(x1, x3), d13 = F::template mul_i<SIGN>(F::sub_l(x1, x3));
+  if (INNER) {
+    x0 = F::add_l(s02, s13);
+    x2 = F::sub_l(s02, s13);
+    x1 = F::add_l(d02, d13);
+    x3 = F::sub_l(d02, d13);
+  } else {
+    x0 = F::add(s02, s13);
+    x2 = F::sub(s02, s13);
+    x1 = F::add(d02, d13);
+    x3 = F::sub(d02, d13);
+  }
 }
 
 template <int SIGN, typename P, typename C>
@@ -197,8 +237,8 @@ __device__ __forceinline__ void fft8(C* v) {
   typedef FT<P> F;
   C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
   C o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
-  fft4<SIGN, P>(e0, e1, e2, e3);
-  fft4<SIGN, P>(o0, o1, o2, o3);
+  fft4<SIGN, P, true>(e0, e1, e2, e3);
+  fft4<SIGN, P, true>(o0, o1, o2, o3);
   C t1 = F::template w8_1<SIGN>(o1);
   C t2 = F::template mul_i<SIGN>(o2);
   C t3 = F::template w8_3<SIGN>(o3);
