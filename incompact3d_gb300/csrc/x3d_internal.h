@@ -205,7 +205,10 @@ bool rhs_axis_fast_ok(const Ctx* c, int axis, const int* dims);
 // X3D_ERR_UNSUPPORTED where stag_fast_ok is false or the pair is not one of
 // those.
 bool stag_fast_ok(const Ctx* c, int axis, const int* dims);
-int stag_one(Ctx* c, OpPlan* p, float* out, const float* in, const int* dims, cudaStream_t st);
+// cor_h / cor_l (x lines only): instead of writing out, subtract the result
+// from the double-float pair (cor_h, cor_l), the fused cor_vel of the step.
+int stag_one(Ctx* c, OpPlan* p, float* out, const float* in, const int* dims, cudaStream_t st,
+             float* cor_h = nullptr, float* cor_l = nullptr);
 int stag_sum(Ctx* c, OpPlan* pA, const float* inA, OpPlan* pB, const float* inB, void* out, bool out64,
              const int* dims, cudaStream_t st);
 int stag_dual(Ctx* c, OpPlan* pA, float* outA, OpPlan* pB, float* outB, const float* in, const int* dims,

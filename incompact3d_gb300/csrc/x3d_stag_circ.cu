@@ -20,6 +20,7 @@
 #include <cstdint>
 
 #include "x3d_circ.cuh"
+#include "x3d_df.cuh"
 
 namespace x3d {
 namespace lk {
@@ -33,6 +34,7 @@ struct StArgs {
   long long sa, sb;        // line and plane offsets
   int rs, na;              // row stride (y/z), lines per plane
   CircOp A, B;
+  float *ch, *cl;          // x lines: (ch, cl) -= result instead of writing out0
 };
 
 // ---- x lines: one warp per line, one solve -----------------------------------
@@ -67,6 +69,23 @@ __global__ void __launch_bounds__(32 * SXW) stag_x(const __grid_constant__ StArg
 #pragma unroll
   for (int j = 0; j < L + LO + HI; ++j) w[j] = bq[hoff<L>(j - LO)];
   circ_warp<K, L>(w, v, p.A, lane);
+  if (p.ch) {
+    // pressure correction of a double-float velocity component (cor_vel):
+    // the same two-sum update as a separate pass over the stored gradient
+    float4* hp = reinterpret_cast<float4*>(p.ch + off + L * lane);
+    float4* lp = reinterpret_cast<float4*>(p.cl + off + L * lane);
+#pragma unroll
+    for (int k4 = 0; k4 < L / 4; ++k4) {
+      float4 h = hp[k4], l = lp[k4];
+      df_add_f(h.x, l.x, -v[4 * k4]);
+      df_add_f(h.y, l.y, -v[4 * k4 + 1]);
+      df_add_f(h.z, l.z, -v[4 * k4 + 2]);
+      df_add_f(h.w, l.w, -v[4 * k4 + 3]);
+      hp[k4] = h;
+      lp[k4] = l;
+    }
+    return;
+  }
   float4* dst = reinterpret_cast<float4*>(reinterpret_cast<float*>(p.out0) + off + L * lane);
 #pragma unroll
   for (int k4 = 0; k4 < L / 4; ++k4) dst[k4] = make_float4(v[4 * k4], v[4 * k4 + 1], v[4 * k4 + 2], v[4 * k4 + 3]);
@@ -257,7 +276,8 @@ bool stag_fast_ok(const Ctx* c, int axis, const int* dims) {
   return (long long)n * rs < (1LL << 31);
 }
 
-int stag_one(Ctx* c, OpPlan* p, float* out, const float* in, const int* dims, cudaStream_t st) {
+int stag_one(Ctx* c, OpPlan* p, float* out, const float* in, const int* dims, cudaStream_t st, float* cor_h,
+             float* cor_l) {
   StArgs a;
   std::memset(&a, 0, sizeof(a));
   dim3 g;
@@ -266,8 +286,14 @@ int stag_one(Ctx* c, OpPlan* p, float* out, const float* in, const int* dims, cu
   if (rc != X3D_OK) return rc;
   a.in0 = in;
   a.out0 = out;
+  if (cor_h || cor_l) {
+    if (p->axis != 0 || !cor_h || !cor_l) return X3D_ERR_UNSUPPORTED;
+    if (!aligned(cor_h, 16) || !aligned(cor_l, 16)) return X3D_ERR_UNSUPPORTED;
+    a.ch = cor_h;
+    a.cl = cor_l;
+  }
   if (p->axis == 0) {
-    if (!aligned(out, 16)) return X3D_ERR_UNSUPPORTED;
+    if (!a.ch && !aligned(out, 16)) return X3D_ERR_UNSUPPORTED;
     if (L == 4) return run_x_kind<4>(p->kind, a, g, st);
     if (L == 8) return run_x_kind<8>(p->kind, a, g, st);
     return run_x_kind<16>(p->kind, a, g, st);

@@ -13,6 +13,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "x3d_df.cuh"
 #include "x3d_internal.h"
 
 namespace x3d {
@@ -45,19 +46,6 @@ __global__ void k_intt64(double* u, const double* h1, const double* h2, const do
   }
 }
 
-// Mixed precision keeps the velocity as a double-float pair (hi, lo) of
-// binary32 arrays: hi is exactly the FP32 operand the operators read, and the
-// pair carries ~48 significand bits, so the state is accumulated to FP64-class
-// accuracy with FP32 instructions only (GB300's FP64 pipe is 1/64 of FP32).
-__device__ __forceinline__ void df_add_f(float& h, float& l, float b) {
-  const float s = __fadd_rn(h, b);
-  const float v = __fsub_rn(s, h);
-  float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, v)), __fsub_rn(b, v));
-  e = __fadd_rn(e, l);
-  const float hh = __fadd_rn(s, e);
-  l = __fsub_rn(e, __fsub_rn(hh, s));
-  h = hh;
-}
 
 // AB/RK update of the double-float state: (h,l) += sum(c_k h_k), the increment
 // formed in FP32 (it carries the FP32 accuracy of the right-hand sides).
@@ -740,8 +728,13 @@ static int divergence(SolverImpl* s, const T* ux, const T* uy, const T* uz, void
 
 // gradp of src/navier.f90:386-432 (the wall-gradient storage of the channel
 // case is done by the caller).
+// cor_h / cor_l (binary32 periodic path only): the double-float velocity
+// components are corrected by the last (x-line) kernel of each gradient
+// component instead of writing px, py, pz (*corrected tells which happened).
 template <typename T>
-static int gradp(SolverImpl* s, const T* pp3, T* px, T* py, T* pz, cudaStream_t st) {
+static int gradp(SolverImpl* s, const T* pp3, T* px, T* py, T* pz, cudaStream_t st, float* const* cor_h = nullptr,
+                 float* const* cor_l = nullptr, bool* corrected = nullptr) {
+  if (corrected) *corrected = false;
   Ctx* c = s->c;
   const int ny = c->grid.ny, nz = c->grid.nz;
   const int nxm = c->ax[0].nm, nym = c->ax[1].nm, nzm = c->ax[2].nm;
@@ -763,9 +756,16 @@ static int gradp(SolverImpl* s, const T* pp3, T* px, T* py, T* pz, cudaStream_t 
     RC(stag_dual(c, zi, f3, zd, (float*)pgz3, (const float*)pp3, d3, st));  // ppi3, pgz3
     RC(stag_dual(c, yi, f2, yd, fy, f3, d3, st));                 // ppi2, pgy2
     RC(op<T>(s, 1, K_IPV, 1, pgzi2, pgz3, d3, st));                // pgzi2
-    RC(stag_one(c, xd, (float*)px, f2, d3, st));
-    RC(stag_one(c, xi, (float*)py, fy, d3, st));
-    RC(stag_one(c, xi, (float*)pz, fzi, d3, st));
+    if (cor_h && cor_l) {
+      RC(stag_one(c, xd, nullptr, f2, d3, st, cor_h[0], cor_l[0]));
+      RC(stag_one(c, xi, nullptr, fy, d3, st, cor_h[1], cor_l[1]));
+      RC(stag_one(c, xi, nullptr, fzi, d3, st, cor_h[2], cor_l[2]));
+      if (corrected) *corrected = true;
+    } else {
+      RC(stag_one(c, xd, (float*)px, f2, d3, st));
+      RC(stag_one(c, xi, (float*)py, fy, d3, st));
+      RC(stag_one(c, xi, (float*)pz, fzi, d3, st));
+    }
     s->launches += 5;
     return X3D_OK;
   }
@@ -1065,12 +1065,17 @@ static int substep(SolverImpl* s, int itr, cudaStream_t st) {
     }
   }
   s->launches += 5;
-  RC(gradp<T>(s, pin, w[0], w[1], w[2], st));
+  bool corrected = false;
+  if (mixed && !s->walls)
+    RC(gradp<T>(s, pin, w[0], w[1], w[2], st, s->uh, s->ul, &corrected));
+  else
+    RC(gradp<T>(s, pin, w[0], w[1], w[2], st));
   if (s->walls) {
     k_wallgrad<<<pw_blocks(c, (long long)c->grid.nx * c->grid.nz), 256, 0, st>>>(
         s->wall_dp, (const double*)w[0], (const double*)w[2], g, c->grid.nx, c->grid.ny, c->grid.nz);
     s->launches++;
   }
+  if (corrected) return cuda_status(cudaGetLastError());  // cor_vel done by the gradient kernels
   if (mixed) {
     Cor3 a;
     for (int q = 0; q < 3; ++q) {
