@@ -40,7 +40,9 @@ struct StArgs {
 // ---- x lines: one warp per line, one solve -----------------------------------
 constexpr int SXW = 8;  // warps (lines) per block
 
-template <int L, int K>
+// COR: the correction mode (p.ch, p.cl set), a separate instantiation so the
+// plain kernel keeps its register count.
+template <int L, int K, bool COR>
 __global__ void __launch_bounds__(32 * SXW) stag_x(const __grid_constant__ StArgs p) {
   extern __shared__ __align__(16) float sxm[];
   constexpr int N = 32 * L, NB = xbuf<L>(), STEP = 32 + 32 / L;
@@ -51,6 +53,9 @@ __global__ void __launch_bounds__(32 * SXW) stag_x(const __grid_constant__ StArg
   float* sq = sxm + (size_t)warp * NB;
   const long long off = (long long)line * p.sa + (long long)blockIdx.y * p.sb;
   const int st0 = lane + lane / L + L + 1;
+  // correction mode: this lane's L points of the state are loaded while the
+  // line is staged, so their latency is not exposed after the solve
+  float4 ch4[COR ? L / 4 : 1], cl4[COR ? L / 4 : 1];
   {
     const float* g = p.in0 + off;
 #pragma unroll
@@ -61,6 +66,15 @@ __global__ void __launch_bounds__(32 * SXW) stag_x(const __grid_constant__ StArg
       cp_async4(sq + d, g + gi);
     }
     cp_async_commit();
+    if (COR) {
+      const float4* hp = reinterpret_cast<const float4*>(p.ch + off + L * lane);
+      const float4* lp = reinterpret_cast<const float4*>(p.cl + off + L * lane);
+#pragma unroll
+      for (int k4 = 0; k4 < L / 4; ++k4) {
+        ch4[k4] = hp[k4];
+        cl4[k4] = lp[k4];
+      }
+    }
     cp_async_wait<0>();
     __syncwarp();
   }
@@ -69,14 +83,14 @@ __global__ void __launch_bounds__(32 * SXW) stag_x(const __grid_constant__ StArg
 #pragma unroll
   for (int j = 0; j < L + LO + HI; ++j) w[j] = bq[hoff<L>(j - LO)];
   circ_warp<K, L>(w, v, p.A, lane);
-  if (p.ch) {
+  if (COR) {
     // pressure correction of a double-float velocity component (cor_vel):
     // the same two-sum update as a separate pass over the stored gradient
     float4* hp = reinterpret_cast<float4*>(p.ch + off + L * lane);
     float4* lp = reinterpret_cast<float4*>(p.cl + off + L * lane);
 #pragma unroll
     for (int k4 = 0; k4 < L / 4; ++k4) {
-      float4 h = hp[k4], l = lp[k4];
+      float4 h = ch4[k4], l = cl4[k4];
       df_add_f(h.x, l.x, -v[4 * k4]);
       df_add_f(h.y, l.y, -v[4 * k4 + 1]);
       df_add_f(h.z, l.z, -v[4 * k4 + 2]);
@@ -199,8 +213,10 @@ static int launch_dyn(KERN kern, dim3 g, dim3 b, size_t sm, cudaStream_t st, con
 
 template <int L, int K>
 static int run_x(const StArgs& a, dim3 g, cudaStream_t st) {
-  static bool conf = false;
-  return launch_dyn(stag_x<L, K>, g, dim3(32 * SXW), (size_t)SXW * xbuf<L>() * sizeof(float), st, a, conf);
+  static bool conf = false, conf_cor = false;
+  const size_t sm = (size_t)SXW * xbuf<L>() * sizeof(float);
+  if (a.ch) return launch_dyn(stag_x<L, K, true>, g, dim3(32 * SXW), sm, st, a, conf_cor);
+  return launch_dyn(stag_x<L, K, false>, g, dim3(32 * SXW), sm, st, a, conf);
 }
 template <int L>
 static int run_x_kind(int kind, const StArgs& a, dim3 g, cudaStream_t st) {
