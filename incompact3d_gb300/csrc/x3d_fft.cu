@@ -81,7 +81,9 @@ __device__ __forceinline__ df df_add_l(df a, df b) {
 __device__ __forceinline__ df df_sub_l(df a, df b) { return df_add_l(a, df_neg(b)); }
 // x.h*y.h + u.h*v.h (sg = +1) or x.h*y.h - u.h*v.h (sg = -1) with the exact
 // product errors and the cross terms folded into one lo sum, then one
-// renormalisation: the real or imaginary part of a complex product.
+// renormalisation: the real or imaginary part of a complex product in 19
+// binary32 operations instead of 25, within a few 2^-48 of |a||b| (about
+// 1.5x the error of separately renormalised products).
 template <int SG>
 __device__ __forceinline__ df df_dot2(df x, df y, df u, df v) {
   const float p1 = __fmul_rn(x.h, y.h);

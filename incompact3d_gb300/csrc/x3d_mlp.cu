@@ -481,6 +481,8 @@ int x3d_mlp_status(x3d_mlp* h) {
   Mlp* m = reinterpret_cast<Mlp*>(h);
   if (!m->tc_err) return X3D_OK;
   int e = 0;
+  // inference may run on any stream, blocking or not: wait for all of them
+  if (cudaDeviceSynchronize() != cudaSuccess) return X3D_ERR_CUDA;
   if (cudaMemcpy(&e, m->tc_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return X3D_ERR_CUDA;
   return e ? X3D_ERR_CUDA : X3D_OK;
 }
