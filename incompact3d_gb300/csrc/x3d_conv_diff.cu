@@ -164,10 +164,6 @@ __global__ void __launch_bounds__(CP* FC, (CP * FC <= 512) ? 2 : 1) conv_diff_yz
       cp_async8(sa + d, p.ua + g);
     }
     cp_async_commit();
-    // a1 is read only in the epilogue: its rows (64 bytes each, one per
-    // thread) are brought into L2 while the slab loads, so that read does not
-    // wait on DRAM after the solves
-    if (p.a1 && t < N) asm volatile("prefetch.global.L2 [%0];" ::"l"(p.a1 + pb + (long long)t * rs));
     cp_async_wait<0>();
     __syncthreads();
   }
