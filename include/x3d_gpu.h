@@ -209,9 +209,11 @@ int x3d_conv_diff_f32(x3d_ctx* ctx, int axis, int q, float* out, const float* uj
 /* Host-side description of the plan x3d_apply uses for (axis, op, npaire,
  * coefset): the line kernel's interior coefficients, Thomas factors,
  * chunked-solve fix-up factors, Sherman-Morrison vector and boundary-row
- * table (layout documented in incompact3d_gb300/csrc/x3d_internal.h).  No
- * device work; returns the output line length or a negative status.  Has no
- * counterpart in the reference (diagnostics). */
+ * table (layout documented in incompact3d_gb300/csrc/x3d_internal.h);
+ * scalars[13] is 1 when the periodic system is the circulant [alpha, 1,
+ * alpha] and the circulant-form kernels solve it.  No device work; returns
+ * the output line length or a negative status.  Has no counterpart in the
+ * reference (diagnostics). */
 int x3d_plan_info(x3d_ctx* ctx, int axis, int op, int npaire, int coefset, double* scalars, double* vecs,
                   double* brows);
 

@@ -301,7 +301,8 @@ int plan_info(Ctx* c, int axis, int kind, int npaire, int coefset, double* sc, d
   if (p->kind == K_DER2 && p->cc == 0.0 && p->cd == 0.0) nt = 2;
   if ((p->kind == K_IVP || p->kind == K_IPV) && p->cd == 0.0) nt = 3;
   const double v[16] = {(double)p->nin, (double)n, (double)p->L, p->periodic ? 1.0 : 0.0, p->ca, p->cb, p->cc,
-                        p->cd, p->alpha, p->den, (double)p->nbrows, (double)nt, (double)CHUNKS, 0, 0, 0};
+                        p->cd, p->alpha, p->den, (double)p->nbrows, (double)nt, (double)CHUNKS,
+                        (p->periodic && plan_is_circulant(p)) ? 1.0 : 0.0, 0, 0};
   if (sc) std::memcpy(sc, v, sizeof(v));
   const dvec* parts[6] = {&p->s, &p->f, &p->w, &p->pf, &p->qb, &p->rsm};
   if (vecs)

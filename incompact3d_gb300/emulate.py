@@ -27,7 +27,7 @@ def plan(ctx, axis, op, npaire, coefset=-1):
                    "x3d_plan_info")
     p = dict(nin=int(sc[0]), nout=int(sc[1]), L=int(sc[2]), periodic=bool(sc[3]), ca=sc[4], cb=sc[5],
              cc=sc[6], cd=sc[7], alpha=sc[8], den=sc[9], nbrows=int(sc[10]), nterms=int(sc[11]),
-             chunks=int(sc[12]))
+             chunks=int(sc[12]), circulant=bool(sc[13]))
     for q, name in enumerate(("s", "f", "w", "pf", "qb", "rsm")):
         p[name] = vec[q * n:(q + 1) * n].copy()
     rows = {}
@@ -126,6 +126,60 @@ def line(op, p, u):
         sx = (t[..., 0] - p["alpha"] * t[..., nout - 1]) / p["den"]
         t = t - sx[..., None] * p["rsm"]
     return t
+
+
+def circ_coefs(p, L, lim=2.0 ** -60, max_carries=64):
+    """Circulant form of a periodic plan for chunks of L rows: the factor mu of
+    I + alpha (S + S^-1) = (I + mu S)(I + mu S^-1) / (1 + mu^2), the chunk
+    multiplier A = (-mu)^L and the number J of cyclic carries kept (the
+    weights |A|^(j-1) above lim), as the host fills them for the kernels."""
+    al = p["alpha"]
+    mu = 2.0 * al / (1.0 + np.sqrt(1.0 - 4.0 * al * al))
+    A = (-mu) ** L
+    J = 1
+    w = abs(A)
+    while J < max_carries and w >= lim:
+        J += 1
+        w *= abs(A)
+    return mu, A, J
+
+
+def line_circ(op, p, u, L, lim=2.0 ** -60):
+    """The circulant-form solve of the fast kernels (x3d_circ.cuh and the
+    generic kernel's periodic branch) on a batch of periodic lines
+    u[..., n], n a multiple of L: right-hand side with coefficients scaled by
+    1 + mu^2, chunk-local forward recurrence z_i = b_i - mu z_(i-1), cyclic
+    carries between chunks (J terms), fix-up (-mu)^(k+1) * carry; the same
+    backwards with x_i = z_i - mu x_(i+1) and (-mu)^(L-k)."""
+    n = p["nout"]
+    if n % L or not p["periodic"]:
+        raise ValueError("line_circ: periodic lines of a multiple of L rows only")
+    mu, A, J = circ_coefs(p, L, lim)
+    sc = 1.0 + mu * mu
+    ps = dict(p, ca=p["ca"] * sc, cb=p["cb"] * sc, cc=p["cc"] * sc, cd=p["cd"] * sc)
+    C = n // L
+    t = np.stack([_interior(op, lambda i: u[..., i % n], r, ps) for r in range(n)], axis=-1)
+    t = t.reshape(u.shape[:-1] + (C, L))
+    for k in range(L):  # forward, chunk-local
+        if k:
+            t[..., k] = t[..., k] - mu * t[..., k - 1]
+    end = t[..., L - 1].copy()
+    carry = np.zeros_like(end)
+    for j in range(1, J + 1):
+        carry += A ** (j - 1) * np.roll(end, j, axis=-1)
+    pw = (-mu) ** (np.arange(L) + 1)
+    t += carry[..., None] * pw
+    for k in range(L - 2, -1, -1):  # backward, chunk-local
+        t[..., k] = t[..., k] - mu * t[..., k + 1]
+    start = t[..., 0].copy()
+    # the backward pass above ran on the fixed-up z; its carries come from the
+    # chunk starts to the right
+    carry = np.zeros_like(start)
+    for j in range(1, J + 1):
+        carry += A ** (j - 1) * np.roll(start, -j, axis=-1)
+    qw = (-mu) ** (L - np.arange(L))
+    t += carry[..., None] * qw
+    return t.reshape(u.shape[:-1] + (n,))
 
 
 def apply(ctx, axis, op, npaire, u, coefset=-1):
