@@ -594,7 +594,26 @@ def run_freeslip(args):
            "launches_per_step": s.lib.x3d_solver_launches_per_step(s.h),
            "stats_row": [(itime - 1) * dt] + [float(v) for v in st]}
     s.close()
+    if not args.no_cpu:
+        out["cpu_baseline"] = freeslip_cpu_baseline(np, n, L, dt)
     print(json.dumps(out), flush=True)
+
+
+def freeslip_cpu_baseline(np, n, L, dt, steps=4):
+    """The oracle on the same free-slip case (RK3, FP64) on all host cores."""
+    import oracle
+    oracle.build()
+    threads = oracle.Oracle.set_threads(os.cpu_count() or 1)
+    o = oracle.Oracle(n, n, n, L, L, L, bc=((1, 1), (1, 1), (1, 1)))
+    x = np.arange(n) * (L / (n - 1))
+    X, Y, Z = x[None, None, :], x[None, :, None], x[:, None, None]
+    ic = (np.sin(X) * np.cos(Y) * np.cos(Z), -np.cos(X) * np.sin(Y) * np.cos(Z), np.zeros((n, n, n)))
+    o.run(*ic, 1, dt, 1 / 1600.0, itimescheme=5, every=1)
+    t0 = time.perf_counter()
+    o.run(*ic, steps, dt, 1 / 1600.0, itimescheme=5, every=steps)
+    sec = time.perf_counter() - t0
+    return {"value": round(n ** 3 * steps / sec / 1e6, 4), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"oracle on the same {n}^3 free-slip case, {steps} RK3 steps"}
 
 
 def run_les_mlp(args):

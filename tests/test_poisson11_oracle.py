@@ -42,3 +42,12 @@ def test_oracle_reproduces_reference_directly_on_the_freeslip_box(oracle_mod):
     rel = np.abs(rows[:, 1:] - GOLD64[:5, 1:]) / np.abs(GOLD64[:5, 1:])
     assert np.all(rel < 1e-10), rel
     assert divmax < 1e-11
+
+
+def test_freeslip_bench_cpu_leg_times_the_oracle_on_the_same_case(oracle_mod):
+    """bench.py --workload freeslip reports the oracle on the same free-slip
+    box beside the GPU rate (here on a small grid, one step)."""
+    import bench
+    out = bench.freeslip_cpu_baseline(np, 17, np.pi, 0.005, steps=1)
+    assert out["kind"] == "port" and out["cores"] >= 1 and out["value"] > 0
+    assert "17^3 free-slip" in out["sample"]
