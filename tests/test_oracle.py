@@ -7,7 +7,9 @@
 * Dirichlet closures reproduce low-order polynomials exactly;
 * the projection of solve_poisson leaves a divergence at round-off level
   (src/navier.f90:257-372, README claim "div u at machine precision");
-* TGV invariants: E_k(0) = 1/8, the Re=1600 decay over the first steps.
+* TGV invariants: E_k(0) = 1/8, the Re=1600 decay over the first steps;
+* the 2-D TGV space-time discrete damping (compute_tgv2D_errors,
+  src/Case-TGV.f90:827-924).
 """
 import numpy as np
 import pytest
@@ -143,3 +145,57 @@ def test_tgv_initial_energy_and_decay(oracle_mod):
     # dE/dt = -eps (energy balance of the semi-discrete system, loose)
     dedt = (rows[1, 1] - rows[0, 1]) / 0.05
     assert dedt == pytest.approx(-rows[:, 2].mean(), rel=0.05)
+
+
+def _k2(s, k):
+    """Modified wavenumber squared of the second derivative (compute_k2,
+    src/Case-TGV.f90:928-950)."""
+    d = s["d"]
+    k2 = (s["asi"] * 2 * (1 - np.cos(k * d)) + 4 * s["bsi"] * 0.5 * (1 - np.cos(2 * k * d))
+          + 9 * s["csi"] * (2 / 9) * (1 - np.cos(3 * k * d)) + 16 * s["dsi"] * (1 / 8) * (1 - np.cos(4 * k * d)))
+    return k2 / (1 + 2 * s["alsai"] * np.cos(k * d))
+
+
+def _ab_decay(lam, dt, nsteps):
+    """Amplitude of y' = -lam y after nsteps of the AB3 scheme with its Euler
+    and AB2 start-up (src/time_integrators.f90:86-100)."""
+    a, f = 1.0, []
+    for it in range(nsteps):
+        f.insert(0, -lam * a)
+        if it == 0:
+            inc = f[0]
+        elif it == 1:
+            inc = 1.5 * f[0] - 0.5 * f[1]
+        else:
+            inc = 23 / 12 * f[0] - 16 / 12 * f[1] + 5 / 12 * f[2]
+        a += dt * inc
+    return a
+
+
+@pytest.mark.parametrize("n,nu,dt,nsteps", [(32, 0.1, 0.001, 1), (32, 0.1, 0.001, 50), (64, 0.1, 0.002, 50),
+                                            (32, 1 / 1600.0, 0.005, 40)])
+def test_tgv2d_space_time_discrete_damping(oracle_mod, n, nu, dt, nsteps):
+    """The 2-D TGV check of the reference (compute_tgv2D_errors,
+    src/Case-TGV.f90:827-924): u = sin x cos y, v = -cos x sin y stays that
+    single mode, its amplitude decays by 1 - 2 k2 dt nu per explicit Euler
+    step (the space-time discrete damping, k2 from compute_k2 at k = 1), and
+    by the same AB2 / AB3 recurrence on -2 nu k2 after the start-up; the
+    analytic exp(-2 nu t) is met to the scheme's truncation error."""
+    nz = 8
+    o = oracle_mod.Oracle(n, n, nz, L, L, L)
+    x = np.arange(n) * L / n
+    X, Y = x[None, None, :], x[None, :, None]
+    mode = np.sin(X) * np.cos(Y)
+    ux = np.broadcast_to(mode, (nz, n, n)).copy()
+    uy = np.broadcast_to(-np.cos(X) * np.sin(Y), (nz, n, n)).copy()
+    uz = np.zeros((nz, n, n))
+    a, b, c, rows, dmax = o.run(ux, uy, uz, nsteps, dt, nu, 3, nsteps)
+    amp = float((a * mode).sum() / (mode * mode).sum() / nz)
+    lam = 2 * nu * _k2(o.scalars(0), 1.0)
+    if nsteps == 1:
+        assert abs(amp - (1 - lam * dt)) < 1e-14
+    assert abs(amp - _ab_decay(lam, dt, nsteps)) < 1e-13
+    assert np.abs(a - amp * mode).max() < 1e-13            # still the single mode
+    assert np.abs(b + amp * np.cos(X) * np.sin(Y)).max() < 1e-13
+    assert np.abs(c).max() < 1e-13
+    assert abs(amp - np.exp(-2 * nu * nsteps * dt)) < 1e-7
