@@ -208,6 +208,7 @@ __global__ void __launch_bounds__(TC_M, TC_CTAS_PER_SM) k_mlp_tc(const __grid_co
   }
   int bad = __syncthreads_or(!mbar_wait(bar_w, 0));
   uint32_t ph = 0;
+  int pend = -1;  // thread 0: parity of an MMA commit whose completion it has not seen
   const long long ntiles = (a.n + TC_M - 1) / TC_M;
   constexpr uint32_t ID64 = idesc_bf16(TC_M, 64), ID16 = idesc_bf16(TC_M, 16);
 
@@ -238,6 +239,7 @@ __global__ void __launch_bounds__(TC_M, TC_CTAS_PER_SM) k_mlp_tc(const __grid_co
       mma_commit(bar_m);
     }
     bad = !mbar_wait(bar_m, ph);
+    if (bad && t == 0) pend = (int)ph;
     ph ^= 1;
     tc_after();
     // layer-1 epilogue: H1 = GELU(D + b1) -> A (K = 64); the MMAs reading A are done
@@ -261,6 +263,7 @@ __global__ void __launch_bounds__(TC_M, TC_CTAS_PER_SM) k_mlp_tc(const __grid_co
       mma_commit(bar_m);
     }
     bad = !mbar_wait(bar_m, ph);
+    if (bad && t == 0) pend = (int)ph;
     ph ^= 1;
     tc_after();
 #pragma unroll 1
@@ -282,6 +285,7 @@ __global__ void __launch_bounds__(TC_M, TC_CTAS_PER_SM) k_mlp_tc(const __grid_co
       mma_commit(bar_m);
     }
     bad = !mbar_wait(bar_m, ph);
+    if (bad && t == 0) pend = (int)ph;
     ph ^= 1;
     tc_after();
     {
@@ -301,9 +305,12 @@ __global__ void __launch_bounds__(TC_M, TC_CTAS_PER_SM) k_mlp_tc(const __grid_co
     bad = __syncthreads_or(bad);
   }
   if (bad) {
-    // a weight copy still in flight is waited for (bounded) before the CTA exits
+    // a weight copy still in flight is waited for (bounded) before the CTA exits,
+    // and so is an MMA group whose completion was not seen, before its
+    // tensor memory is freed
     if (t == 0) {
       mbar_wait(bar_w, 0);
+      if (pend >= 0) mbar_wait(bar_m, (uint32_t)pend);
       atomicExch(a.err, 1);
     }
   }
